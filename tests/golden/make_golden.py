@@ -1,0 +1,266 @@
+"""Generate the golden vectors in tests/golden/*.npz from the reference itself.
+
+Run in a container that has the reference tree (after ``make -C oracle``):
+
+    python tests/golden/make_golden.py
+
+Every number in the fixtures comes from the reference's own Python classes and
+its own compiled stencils (see ``ref_harness.py`` for how they are imported).
+The fixtures pin both the oracle (``oracle/spde_oracle.py``) and, through it,
+the CUDA path.  Cases:
+
+* ``stencil_*``  raw COO triplets (with the ``row == M*N`` sentinel) of the four
+  stencil families ``AcH/AH/Acw/Aw`` for bc 1 and 3 and every ``diff`` mode
+  (reference ``spdes/ccode/*.cpp``).
+* ``model_*``    one model object each: the precision Q (CSR), the objective
+  ``logLike(par, grad=False)`` and the Hutchinson gradient
+  ``logLike(par, nh1, grad=True)`` with ``np.random.seed`` fixed before the call
+  (reference e.g. ``spdes/advection_diffusion2D.py:187-223``).
+* ``facade_wm``  ``Model.update`` conditional mean (reference ``model.py:120-127``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+from scipy import sparse
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import ref_harness  # noqa: E402
+
+OUT = HERE
+NH1 = 20
+SEED_V = 1234
+
+
+def _stencil_cases():
+    lib_dir = ref_harness.REF_LIBS
+    M, N, hx, hy = 7, 6, 1.3, 0.8
+    rng = np.random.default_rng(7)
+    H = rng.normal(size=(M * N, 4, 2, 2))
+    H = H + H.transpose(0, 1, 3, 2)  # symmetric per face, as the models build them
+    Hc = np.array([[1.3, 0.4], [0.4, 0.7]])
+    G = rng.normal(size=(M * N, 4))
+    G[3, 1] = 0.0  # exercise the G/|G| = NaN path of the derivative modes
+    dG = rng.normal(size=(M * N, 4))
+    Gc = np.array([0.3, -0.2])
+    out = {}
+    c_int, c_dbl = ctypes.c_int, ctypes.c_double
+    for bc in (1, 3):
+        for fam in ("AcH", "AH"):
+            lib = ctypes.cdll.LoadLibrary(os.path.join(lib_dir, f"lib_{fam}_2D_b{bc}.so"))
+            lib.AH_new.restype = ctypes.c_void_p
+            for f in ("AH_Row", "AH_Col", "AH_Val"):
+                getattr(lib, f).argtypes = [ctypes.c_void_p]
+            lib.AH_Row.restype = np.ctypeslib.ndpointer(dtype=np.int32, shape=(9 * M * N,))
+            lib.AH_Col.restype = np.ctypeslib.ndpointer(dtype=np.int32, shape=(9 * M * N,))
+            lib.AH_Val.restype = np.ctypeslib.ndpointer(dtype=np.float64, shape=(9 * M * N,))
+            lib.AH_delete.argtypes = [ctypes.c_void_p]
+            Hin = np.ascontiguousarray(Hc if fam == "AcH" else H.copy())
+            lib.AH_new.argtypes = [c_int, c_int, np.ctypeslib.ndpointer(dtype=np.float64, shape=Hin.shape),
+                                   c_dbl, c_dbl]
+            obj = lib.AH_new(M, N, Hin, hx, hy)
+            key = f"{fam}_b{bc}"
+            out[key + "_row"] = lib.AH_Row(obj).copy()
+            out[key + "_col"] = lib.AH_Col(obj).copy()
+            out[key + "_val"] = lib.AH_Val(obj).copy()
+            lib.AH_delete(obj)
+        for fam in ("Acw", "Aw"):
+            lib = ctypes.cdll.LoadLibrary(os.path.join(lib_dir, f"lib_{fam}_2D_b{bc}.so"))
+            lib.Aw_new.restype = ctypes.c_void_p
+            for f in ("Aw_Row", "Aw_Col", "Aw_Val"):
+                getattr(lib, f).argtypes = [ctypes.c_void_p]
+            lib.Aw_Row.restype = np.ctypeslib.ndpointer(dtype=np.int32, shape=(5 * M * N,))
+            lib.Aw_Col.restype = np.ctypeslib.ndpointer(dtype=np.int32, shape=(5 * M * N,))
+            lib.Aw_Val.restype = np.ctypeslib.ndpointer(dtype=np.float64, shape=(5 * M * N,))
+            lib.Aw_delete.argtypes = [ctypes.c_void_p]
+            for diff in (1, 2, 3):
+                if fam == "Acw":
+                    Gin = np.ascontiguousarray(Gc)
+                    lib.Aw_new.argtypes = [c_int, c_int, np.ctypeslib.ndpointer(dtype=np.float64, shape=(2,)),
+                                           c_dbl, c_dbl, c_int]
+                    obj = lib.Aw_new(M, N, Gin, hx, hy, diff)
+                else:
+                    Gin = np.ascontiguousarray(G.copy())
+                    dGin = np.ascontiguousarray(dG.copy())
+                    nd = np.ctypeslib.ndpointer(dtype=np.float64, shape=(M * N, 4))
+                    lib.Aw_new.argtypes = [c_int, c_int, nd, c_dbl, c_dbl, c_int, nd]
+                    obj = lib.Aw_new(M, N, Gin, hx, hy, diff, dGin)
+                key = f"{fam}_b{bc}_d{diff}"
+                out[key + "_row"] = lib.Aw_Row(obj).copy()
+                out[key + "_col"] = lib.Aw_Col(obj).copy()
+                out[key + "_val"] = lib.Aw_Val(obj).copy()
+                lib.Aw_delete(obj)
+    np.savez_compressed(os.path.join(OUT, "stencils.npz"), M=M, N=N, hx=hx, hy=hy, H=H, Hc=Hc, G=G, dG=dG,
+                        Gc=Gc, **out)
+
+
+def _csr(Q):
+    Q = sparse.csr_matrix(Q)
+    Q.sort_indices()
+    return dict(Q_data=Q.data, Q_indices=Q.indices.astype(np.int32), Q_indptr=Q.indptr.astype(np.int64))
+
+
+def _simulate(Q, S, noise_sd, seed):
+    rng = np.random.default_rng(seed)
+    L = np.linalg.cholesky(Q.toarray())
+    import scipy.linalg as sla
+    x = sla.solve_triangular(L.T, rng.normal(size=Q.shape[0]), lower=False)
+    return S @ x + noise_sd * rng.normal(size=S.shape[0])
+
+
+def _model_case(name, mod, par, idx, noise_sd, gridinfo, extra=None):
+    Q = mod.Q if mod.Q is not None else mod.makeQ(par, grad=False)[0]
+    S = mod.grid.getS(idx)
+    y = _simulate(Q, S, noise_sd, seed=11)
+    mod.initFit(y, idx=idx)
+    f = mod.logLike(par, grad=False)
+    np.random.seed(SEED_V)
+    fg, jac = mod.logLike(par, nh1=NH1, grad=True)
+    rec = dict(par=np.asarray(par, float), idx=np.asarray(idx, np.int64), y=y, f=f, f_grad=fg, jac=jac,
+               nh1=NH1, seed_v=SEED_V, **_csr(Q), **gridinfo)
+    if extra:
+        rec.update(extra)
+    np.savez_compressed(os.path.join(OUT, f"model_{name}.npz"), **rec)
+    print(f"{name}: n={Q.shape[0]} nnz={Q.nnz} f={f:.12g} |jac|={np.linalg.norm(jac):.6g}")
+
+
+def _st_grid(sp, M, N, T, Nbs=3, extend=None):
+    g = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float), t=np.arange(T, dtype=float),
+                extend=extend, Nbs=Nbs)
+    return g, dict(M=M, N=N, T=T, Nbs=Nbs, extend=-1 if extend is None else extend)
+
+
+def _sp_grid(sp, M, N, Nbs=3):
+    g = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float), Nbs=Nbs)
+    return g, dict(M=M, N=N, T=1, Nbs=Nbs, extend=-1)
+
+
+def _mod0(sp, M, N, ani, ha, bc):
+    g0 = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float))
+    return sp.spde_init(model="whittle-matern", grid=g0, ani=ani, ha=ha, bc=bc)
+
+
+def _smooth_ww(grid, seed):
+    rng = np.random.default_rng(seed)
+    M, N = grid.M, grid.N
+    X, Y = np.meshgrid(np.arange(M), np.arange(N))
+    we = np.zeros(M * N)
+    wn = np.zeros(M * N)
+    for _ in range(4):
+        kx, ky = rng.uniform(0.2, 0.8, size=2)
+        ph = rng.uniform(0, 2 * np.pi, size=2)
+        we += 0.5 * np.cos(kx * X + ky * Y + ph[0]).ravel()
+        wn += 0.5 * np.sin(kx * X - ky * Y + ph[1]).ravel()
+    return grid.assimilate_adv(we, wn)
+
+
+def main():
+    sp = ref_harness.load_reference()
+    _stencil_cases()
+
+    # config-1 shape: stationary anisotropic Whittle-Matern, 40x40, Neumann
+    g, gi = _sp_grid(sp, 40, 40)
+    par = np.array([-0.7, 0.0, 0.0, np.sqrt(np.exp(0.3) - 1.0), 1.0])
+    mod = sp.spde_init(model="whittle-matern", grid=g, parameters=par, ani=True, ha=False, bc=1)
+    idx = np.random.default_rng(0).choice(1600, 200, replace=False)
+    _model_case("wm_ani_bc1", mod, par, idx, 0.1, dict(gi, bc=1, family="whittle-matern", ani=1, ha=0))
+
+    g, gi = _sp_grid(sp, 15, 12)
+    par = np.array([-0.5, 0.2, 1.5])
+    mod = sp.spde_init(model="whittle-matern", grid=g, parameters=par, ani=False, ha=False, bc=3)
+    idx = np.random.default_rng(1).choice(180, 60, replace=False)
+    _model_case("wm_iso_bc3", mod, par, idx, 0.2, dict(gi, bc=3, family="whittle-matern", ani=0, ha=0))
+
+    g, gi = _sp_grid(sp, 14, 13)
+    par = np.array([-0.4, -0.2, 0.3, -0.5, 1.2])
+    mod = sp.spde_init(model="whittle-matern", grid=g, parameters=par, ani=True, ha=True, bc=3)
+    idx = np.random.default_rng(2).choice(182, 70, replace=False)
+    _model_case("wm_ha_bc3", mod, par, idx, 0.2, dict(gi, bc=3, family="whittle-matern", ani=1, ha=1))
+
+    g, gi = _sp_grid(sp, 12, 11)
+    rng = np.random.default_rng(3)
+    par = np.hstack([-0.5 + 0.2 * rng.normal(size=9), 0.1 * rng.normal(size=9), 0.3 * rng.normal(size=9),
+                     0.3 * rng.normal(size=9), 1.0])
+    mod = sp.spde_init(model="var-whittle-matern", grid=g, parameters=par, ani=True, ha=False, bc=1)
+    idx = np.random.default_rng(4).choice(132, 50, replace=False)
+    _model_case("varwm_ani_bc1", mod, par, idx, 0.2, dict(gi, bc=1, family="var-whittle-matern", ani=1, ha=0))
+
+    # config-2 shape (reduced): stationary advection-diffusion with a fitted initial field
+    for bc in (1, 3):
+        M, N, T = 12, 10, 5
+        g, gi = _st_grid(sp, M, N, T)
+        par = np.array([np.log(0.3), np.log(0.5), np.sqrt(0.5), 0.0, 0.3, -0.2, 0.0,
+                        np.log(0.3), np.log(0.5), np.sqrt(0.5), 0.0, np.log(1 / 0.05 ** 2)])
+        mod0 = _mod0(sp, M, N, True, False, bc)
+        mod = sp.spde_init(model="advection-diffusion", grid=g, parameters=par, ani=True, ha=False, bc=bc, mod0=mod0)
+        idx = np.random.default_rng(5).choice(M * N * T, 150, replace=False)
+        _model_case(f"advdiff_ani_bc{bc}", mod, par, idx, 0.05,
+                    dict(gi, bc=bc, family="advection-diffusion", ani=1, ha=0))
+
+    M, N, T = 10, 9, 4
+    g, gi = _st_grid(sp, M, N, T)
+    par = np.array([np.log(0.4), np.log(0.6), 0.4, -0.3, -0.25, 0.15, 0.2, np.log(0.5), np.log(0.7), 0.2, 0.1,
+                    np.log(200.0)])
+    mod0 = _mod0(sp, M, N, True, True, 3)
+    mod = sp.spde_init(model="advection-diffusion", grid=g, parameters=par, ani=True, ha=True, bc=3, mod0=mod0)
+    idx = np.random.default_rng(6).choice(M * N * T, 100, replace=False)
+    _model_case("advdiff_ha_bc3", mod, par, idx, 0.1, dict(gi, bc=3, family="advection-diffusion", ani=1, ha=1))
+
+    M, N, T = 9, 8, 4
+    g, gi = _st_grid(sp, M, N, T)
+    par = np.array([np.log(0.5), np.log(0.8), 0.35, -0.15, 0.1, np.log(0.5), np.log(0.9), np.log(150.0)])
+    mod0 = _mod0(sp, M, N, False, False, 1)
+    mod = sp.spde_init(model="advection-diffusion", grid=g, parameters=par, ani=False, ha=False, bc=1, mod0=mod0)
+    idx = np.random.default_rng(7).choice(M * N * T, 90, replace=False)
+    _model_case("advdiff_iso_bc1", mod, par, idx, 0.1, dict(gi, bc=1, family="advection-diffusion", ani=0, ha=0))
+
+    # config-3 family at Nbs=3: spatially varying diffusion, given velocity field scaled by lambda
+    from spdepy.spdes.cov_advection_var_diffusion2D import CovAdvectionVarDiffusion2D
+    for bc in (1, 3):
+        M, N, T = 11, 10, 4
+        g, gi = _st_grid(sp, M, N, T)
+        ww = _smooth_ww(g, seed=21)
+        rng = np.random.default_rng(22)
+        par = np.hstack([np.log(0.4) + 0.1 * rng.normal(size=9), np.log(0.6) + 0.1 * rng.normal(size=9),
+                         0.3 * rng.normal(size=9), 0.3 * rng.normal(size=9), 0.8, 0.1,
+                         np.log(0.4), np.log(0.6), 0.3, 0.0, np.log(100.0)])
+        mod0 = _mod0(sp, M, N, True, False, bc)
+        mod = CovAdvectionVarDiffusion2D(grid=g, mod0=mod0, par=par, bc=bc, ww=ww)
+        mod.setQ(par)
+        idx = np.random.default_rng(23).choice(M * N * T, 120, replace=False)
+        _model_case(f"covadv_vardiff_bc{bc}", mod, par, idx, 0.1,
+                    dict(gi, bc=bc, family="cov-advection-var-diffusion", ani=1, ha=0), extra=dict(ww=ww))
+
+    M, N, T = 10, 9, 4
+    g, gi = _st_grid(sp, M, N, T)
+    rng = np.random.default_rng(31)
+    par = np.hstack([np.log(0.4) + 0.1 * rng.normal(size=9), np.log(0.6) + 0.1 * rng.normal(size=9),
+                     0.3 * rng.normal(size=9), 0.3 * rng.normal(size=9), 0.2 * rng.normal(size=9),
+                     0.2 * rng.normal(size=9), 0.1, np.log(0.4), np.log(0.6), 0.3, 0.0, np.log(100.0)])
+    mod0 = _mod0(sp, M, N, True, False, 1)
+    mod = sp.spde_init(model="var-advection-var-diffusion", grid=g, parameters=par, ani=True, ha=False, bc=1,
+                       mod0=mod0)
+    idx = np.random.default_rng(32).choice(M * N * T, 100, replace=False)
+    _model_case("varadv_vardiff_bc1", mod, par, idx, 0.1,
+                dict(gi, bc=1, family="var-advection-var-diffusion", ani=1, ha=0))
+
+    # facade: Model.update conditional mean on a small stationary field
+    g, gi = _sp_grid(sp, 16, 14)
+    par = np.array([-0.6, 0.1, 0.2, 0.4, 2.0])
+    model = sp.Model(spde="whittle-matern", grid=g, parameters=par, ani=True, ha=False, bc=3)
+    model.setModel()
+    idx = np.random.default_rng(41).choice(16 * 14, 40, replace=False)
+    yobs = np.random.default_rng(42).normal(size=40)
+    Q0 = model.Q.copy()
+    model.update(yobs, idx)
+    np.savez_compressed(os.path.join(OUT, "facade_wm.npz"), par=par, idx=idx, y=yobs, mu=model.mu,
+                        tau=model.tau, **_csr(Q0), **dict(gi, bc=3))
+    print("facade_wm: mu norm", np.linalg.norm(model.mu))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,53 @@
+"""Pin the oracle against fixtures produced by the reference itself (CPU only)."""
+import numpy as np
+import pytest
+from scipy import sparse
+
+from golden_cases import load, model_cases, oracle_model
+from oracle import stencils as S
+
+
+def test_stencils_bit_exact():
+    g = load("stencils.npz")
+    M, N, hx, hy = int(g["M"]), int(g["N"]), float(g["hx"]), float(g["hy"])
+    for bc in (1, 3):
+        for fam, field in (("AcH", False), ("AH", True)):
+            r, c, v = S.diffusion_triplets(M, N, g["H"] if field else g["Hc"], hx, hy, bc, field)
+            k = f"{fam}_b{bc}"
+            assert np.array_equal(r, g[k + "_row"]) and np.array_equal(c, g[k + "_col"])
+            assert np.array_equal(v, g[k + "_val"])
+        for diff in (1, 2, 3):
+            r, c, v = S.advection_const_triplets(M, N, g["Gc"], hx, hy, bc, diff)
+            k = f"Acw_b{bc}_d{diff}"
+            assert np.array_equal(r, g[k + "_row"]) and np.array_equal(c, g[k + "_col"])
+            assert np.array_equal(v, g[k + "_val"], equal_nan=True)
+            r, c, v = S.advection_field_triplets(M, N, g["G"], hx, hy, bc, diff, g["dG"])
+            k = f"Aw_b{bc}_d{diff}"
+            assert np.array_equal(r, g[k + "_row"]) and np.array_equal(c, g[k + "_col"])
+            assert np.array_equal(v, g[k + "_val"], equal_nan=True)
+
+
+@pytest.mark.parametrize("name", model_cases())
+def test_model_golden(name):
+    g = load(name)
+    mod = oracle_model(g)
+    par = g["par"]
+    Q = mod.makeQ(par)
+    Qg = sparse.csr_matrix((g["Q_data"], g["Q_indices"], g["Q_indptr"]), shape=Q.shape)
+    assert abs(Q - Qg).max() <= 1e-13 * abs(Qg).max()
+    f = mod.loglike(par, g["y"], g["idx"], grad=False)
+    assert abs(f - float(g["f"])) <= 1e-12 * abs(float(g["f"]))
+    fg, jac = mod.loglike(par, g["y"], g["idx"], grad=True, nh1=int(g["nh1"]), seed=int(g["seed_v"]))
+    assert np.allclose(jac, g["jac"], rtol=1e-10, atol=1e-12 * np.abs(g["jac"]).max())
+
+
+def test_facade_update_golden():
+    from oracle.spde_oracle import OracleGrid, OracleModel
+    g = load("facade_wm.npz")
+    grid = OracleGrid(np.arange(int(g["M"]), dtype=float), np.arange(int(g["N"]), dtype=float))
+    mod = OracleModel(grid, "whittle-matern", "ani", int(g["bc"]))
+    Q = mod.makeQ(g["par"])
+    Qg = sparse.csr_matrix((g["Q_data"], g["Q_indices"], g["Q_indptr"]), shape=Q.shape)
+    assert abs(Q - Qg).max() <= 1e-13 * abs(Qg).max()
+    mu = mod.conditional_mean(g["par"], g["y"], g["idx"], tau=float(g["tau"]))
+    assert np.allclose(mu, g["mu"], rtol=1e-11, atol=1e-13)
