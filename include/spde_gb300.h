@@ -1,0 +1,150 @@
+/* spde_gb300: GB300-native inference hot path of spdepy (C ABI).
+ *
+ * Every entry point returns an int status (SPDE_OK = 0), never throws, and runs
+ * on the plan's CUDA stream (the default stream unless spde_plan_set_stream is
+ * called).  Arrays documented as "device" are CUDA device pointers owned by the
+ * caller; "host" arrays are ordinary host memory.  A plan is not thread-safe:
+ * use one plan per host thread.
+ *
+ * Node numbering is the reference's: node k = t*Mx*Ny + j*Mx + i for cell
+ * (i, j) at time t (spdes/advection_diffusion2D.py:112-116), on the grid
+ * including any extension cells.  "Stencil layout" stores nslots values per
+ * node (43 for T > 1: 9 at t-1, 25 at t, 9 at t+1; 25 for T == 1), slot order
+ * dt-major, then dy, then dx, each ascending.
+ */
+#ifndef SPDE_GB300_H
+#define SPDE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPDE_OK 0
+#define SPDE_ERR_ARG 1
+#define SPDE_ERR_CUDA 2
+#define SPDE_ERR_NOT_SPD 3
+#define SPDE_ERR_NO_MEMORY 4
+#define SPDE_ERR_STATE 5
+#define SPDE_ERR_NOT_CONVERGED 6
+
+#define SPDE_PRECISION_FP64 0 /* factor, solves and inverse in FP64 */
+#define SPDE_PRECISION_MIXED 1 /* FP32 factor, FP64 pivots / log-det / refinement */
+
+typedef struct SpdePlan SpdePlan;
+
+typedef struct {
+  int64_t n;            /* nodes */
+  int64_t nfronts;      /* dense fronts (tree nodes of the dissection) */
+  int32_t max_depth;
+  int32_t max_front;    /* largest front order */
+  int32_t nslots;
+  int32_t precision;
+  double factor_flops;  /* algorithmic flops of one factorisation */
+  double selinv_flops;  /* algorithmic flops of one selected inversion */
+  double nnz_l;         /* entries of the dense-front factor */
+  double bytes_factor;  /* device bytes of the factor arena */
+  double bytes_work;    /* device bytes of the update / inverse pools */
+  int64_t launches;     /* kernel launches issued by this plan so far */
+} SpdePlanInfo;
+
+/* Model description (spde_set_model).  Canonical parameter vector theta:
+ *   [0,nk) log kappa | [nk,2nk) log gamma | [2nk,3nk) vx | [3nk,4nk) vy |
+ *   [4nk,4nk+nw) advection | log sigma | log kappa0, log gamma0, vx0, vy0 | log tau
+ * with nk = nbasis if var_h else 1 and nw = 2 (constant velocity), 2*nbasis
+ * (B-spline velocity), 1 (lambda times a given field) or 0 (spatial model).
+ * The last five entries before log tau describe the initial-field
+ * Whittle-Matern model of spatio-temporal models and are ignored when T == 1. */
+typedef struct {
+  int32_t Mx, Ny, T;
+  int32_t bc;           /* 1: Neumann (zero flux), 3: Dirichlet (zero) */
+  double hx, hy, dt;
+  int32_t diff_form;    /* 0: gamma I, 1: gamma I + v v^T, 2: half-angle */
+  int32_t var_h;        /* 0: constant kappa/gamma/v; 1: B-spline fields */
+  int32_t adv;          /* 0 none, 1 constant, 2 B-spline field, 3 lambda * given field */
+  int32_t nbasis;       /* B-spline functions (Nbs^2) */
+  const double* bs;     /* host, Ns x nbasis, cell centres            (var_h) */
+  const double* bsH;    /* host, Ns x 4 x nbasis, faces W,E,S,N        (var_h) */
+  const double* bsA;    /* host, Ns x 4 x nbasis, faces E,N,W,S        (adv == 2) */
+  const double* ww;     /* host, Ns x 4 given face velocities          (adv == 3) */
+  int32_t mod0_diff_form;
+  int32_t mod0_bc;
+} SpdeModelDesc;
+
+/* ---- B3: stencil triplets.  Replace the ctypes calls
+ * AH_new/AH_Row/AH_Col/AH_Val/AH_delete (spdes/ccode/AcH_2D_b1.cpp:170-185,
+ * AH_2D_b1.cpp:154-169) and Aw_new/Aw_Row/Aw_Col/Aw_Val/Aw_delete
+ * (Acw_2D_b1.cpp:117-132, Aw_2D_b1.cpp:136-151).  Outputs are device arrays of
+ * 9*M*N (diffusion) or 5*M*N (advection) triplets with the reference's
+ * row == M*N sentinel; values match the reference's doubles bit for bit.
+ * field = 0: H is one 2x2 (row-major) / G is (wx, wy); field = 1: H is
+ * (M*N, 4, 2, 2) / G and dG are (M*N, 4).  Unlike the reference, inputs are
+ * never modified.  bc must be 1 or 3. */
+int spde_diffusion_triplets(int M, int N, const double* H, int field, double hx, double hy, int bc, int* row,
+                            int* col, double* val, void* stream);
+int spde_advection_triplets(int M, int N, const double* G, const double* dG, int field, double hx, double hy, int bc,
+                            int diff, int* row, int* col, double* val, void* stream);
+
+/* ---- plan: symbolic analysis + device arenas (the analysis half of
+ * sksparse.cholmod.cholesky, called at spdes/advection_diffusion2D.py:117,193). */
+int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out);
+int spde_plan_destroy(SpdePlan* plan);
+int spde_plan_set_stream(SpdePlan* plan, void* stream);
+int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info);
+const char* spde_last_error(const SpdePlan* plan);
+/* Symbolic analysis without a GPU (host only): statistics and the ordering. */
+int spde_symbolic_info(int Mx, int Ny, int T, int leaf_max, SpdePlanInfo* info);
+int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int32_t* front_ns, int32_t* front_nb,
+                         int32_t* front_parent, int64_t nfronts_cap);
+
+/* ---- assembly: makeQ (spdes/advection_diffusion2D.py:86-117,
+ * spdes/var_advection_var_diffusion2D.py:83-116,
+ * spdes/whittle_matern_anisotropic2D.py:59-75). */
+int spde_set_model(SpdePlan* plan, const SpdeModelDesc* desc);
+int spde_assemble(SpdePlan* plan, const double* theta_host, int ntheta);
+/* Q (+ tau S^T S when with_obs) in stencil layout, natural order, device FP64. */
+int spde_export_q(SpdePlan* plan, int with_obs, double tau, double* q_dev);
+/* y = (Q [+ tau S^T S]) x, natural order, nrhs columns row-major, device FP64. */
+int spde_spmv(SpdePlan* plan, int with_obs, double tau, const double* x_dev, double* y_dev, int nrhs);
+
+/* ---- observations: S = selected identity rows (grids/spat2Dtemp_regular_mesh.py:35-58);
+ * idx are node indices (duplicates allowed), host int64. */
+int spde_set_obs(SpdePlan* plan, const int64_t* idx_host, int m);
+
+/* ---- factorisation: cholesky(Q) / cholesky(Q + tau S^T S) and Factor.logdet()
+ * (spdes/advection_diffusion2D.py:117,192-193,198). */
+int spde_factor(SpdePlan* plan, int with_obs, double tau, double* logdet);
+/* Factor.solve_A (spdes/advection_diffusion2D.py:194,201-202; model.py:126):
+ * x = A^-1 b for the factored matrix, device FP64, natural order, nrhs columns
+ * row-major; refine_iters FP64 iterative-refinement steps (stop at rel. residual
+ * <= tol); *resid receives the final relative residual. */
+int spde_solve(SpdePlan* plan, const double* b_dev, double* x_dev, int nrhs, int refine_iters, double tol,
+               double* resid);
+/* Factor.apply_Pt(Factor.solve_Lt(z)) (model.py:80): x = P L^-T z for the factored
+ * matrix; z, x device FP64 natural order (nrhs columns).  With Q = P L L^T P^T the
+ * columns of x are draws from N(0, Q^-1) when z ~ N(0, I). */
+int spde_sample(SpdePlan* plan, const double* z_dev, double* x_dev, int nrhs);
+/* Selected inverse (rqinv.R:18-205 via model.py:89-118): Z = A^-1 on the stencil
+ * pattern, stencil layout, device FP64.  Consumes the factor. */
+int spde_selinv(SpdePlan* plan, double* zq_dev);
+/* d/dtheta <Gbar, Q(theta)> for a symmetric Gbar in stencil layout (device
+ * FP64); grad_host receives ntheta-1 values (all but log tau). */
+int spde_adjoint(SpdePlan* plan, const double* gbar_dev, double* grad_host);
+
+/* ---- log-likelihood and gradient: logLike (spdes/advection_diffusion2D.py:187-223).
+ * y_dev: m x r observations (device FP64, row-major, in spde_set_obs order).
+ * grad_mode: 0 none, 1 exact traces by selected inversion, 2 Hutchinson with the
+ * n x nh1 probe matrix probes_dev (device FP64 entries +-1).  Outputs the
+ * reference's normalised objective f = -like/(m r) and jac = -g/(m r) (ntheta
+ * values, canonical order). */
+int spde_loglike(SpdePlan* plan, const double* theta_host, int ntheta, const double* y_dev, int r, int grad_mode,
+                 const double* probes_dev, int nh1, double* f, double* jac_host);
+/* Conditional mean mu = mu0 + tau (Q + tau S^T S)^-1 S^T (y - S mu0) (model.py:120-127);
+ * y_dev m values, mu0_dev/mu_dev n values (device FP64). */
+int spde_conditional_mean(SpdePlan* plan, double tau, const double* y_dev, const double* mu0_dev, double* mu_dev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPDE_GB300_H */

@@ -69,8 +69,10 @@ def diffusion_triplets(M, N, H, hx, hy, bc, field):
         E10, W10 = H[:, 1, 1, 0], H[:, 0, 1, 0]
     else:
         W00 = np.full(n, H[0, 0]); E00 = W00.copy()
-        N01 = np.full(n, H[1, 0]); S01 = N01.copy()
-        E10 = N01.copy(); W10 = N01.copy()
+        # AcH_2D_b1.cpp:42-49 uses H[1][0] for every cross term; AcH_2D_b3.cpp:41-44
+        # reads H[0][1] on the N/S faces and H[1][0] on the E/W faces
+        N01 = np.full(n, H[1, 0] if bc == 1 else H[0, 1]); S01 = N01.copy()
+        E10 = np.full(n, H[1, 0]); W10 = E10.copy()
         N11 = np.full(n, H[1, 1]); S11 = N11.copy()
     if bc == 1:
         if field:
@@ -97,11 +99,19 @@ def diffusion_triplets(M, N, H, hx, hy, bc, field):
         col = _cols(M, N, i_n, i_p, j_n, j_p, i, j)
         k = j * M + i
         row = np.repeat(k[:, None], 9, axis=1)
-        rem = np.zeros(n)
         fold = col == k[:, None]
         fold[:, 0] = False
-        # AH_2D_b1.cpp:54-101: a folded entry adds its value to `rem` and is dropped
-        rem = (val * fold).sum(axis=1)
+        # AH_2D_b1.cpp:54-101: a folded entry adds its two terms to `rem` (in the
+        # C++ association rem = (rem + a) + b) and is dropped
+        ha, hb = hy / hx, hx / hy
+        terms = [(ha * E00, 0.25 * (N01 - S01)), (ha * W00, -0.25 * (N01 - S01)),
+                 (hb * N11, 0.25 * (E10 - W10)), (hb * S11, -0.25 * (E10 - W10)),
+                 (0.25 * (N01 + E10), None), (0.25 * (S01 + W10), None),
+                 (-0.25 * (N01 + W10), None), (-0.25 * (S01 + E10), None)]
+        rem = np.zeros(n)
+        for p, (a, b) in enumerate(terms, start=1):
+            upd = rem + a if b is None else (rem + a) + b
+            rem = np.where(fold[:, p], upd, rem)
         row = np.where(fold, n, row)
         val[:, 0] = val[:, 0] + rem
         return row.astype(np.int32).ravel(), col.astype(np.int32).ravel(), val.ravel()

@@ -1,0 +1,517 @@
+// C ABI of libspde_gb300 (declared in include/spde_gb300.h).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/spde_gb300.h"
+#include "engine.cuh"
+
+using namespace spde;
+
+
+#define API_CUDA(x)                                                      \
+  do {                                                                   \
+    cudaError_t e_ = (x);                                                \
+    if (e_ != cudaSuccess) {                                             \
+      plan->p.last_error = std::string(#x) + ": " + cudaGetErrorString(e_); \
+      return SPDE_ERR_CUDA;                                              \
+    }                                                                    \
+  } while (0)
+
+namespace {
+
+__global__ void obs_rhs_kernel(const int* __restrict__ idx, int m, int r, double tau, const double* __restrict__ y,
+                               const double* __restrict__ mu0, double* __restrict__ b) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(m) * r) return;
+  const int i = int(e / r), c = int(e % r);
+  const int k = idx[i];
+  double v = y[e];
+  if (mu0) v -= mu0[int64_t(k) * r + c];
+  atomicAdd(&b[int64_t(k) * r + c], tau * v);
+}
+
+// block partial sums of a[i]*b[i] (b == nullptr: a[i]^2)
+__global__ void dot_partial_kernel(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+                                   double* __restrict__ part) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x; i < n; i += int64_t(gridDim.x) * 256)
+    s += b ? a[i] * b[i] : a[i] * a[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// residual of the observations: d[i, c] = y[i, c] - mu[idx_i, c]
+__global__ void obs_resid_kernel(const int* __restrict__ idx, int m, int r, const double* __restrict__ y,
+                                 const double* __restrict__ mu, double* __restrict__ d) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(m) * r) return;
+  d[e] = y[e] - mu[int64_t(idx[e / r]) * r + e % r];
+}
+
+__device__ __forceinline__ void slot_geo(int T, int s, int* dx, int* dy, int* dt) {
+  if (T == 1) { *dt = 0; *dy = s / 5 - 2; *dx = s % 5 - 2; return; }
+  if (s < 9) { *dt = -1; *dy = s / 3 - 1; *dx = s % 3 - 1; }
+  else if (s < 34) { *dt = 0; *dy = (s - 9) / 5 - 2; *dx = (s - 9) % 5 - 2; }
+  else { *dt = 1; *dy = (s - 34) / 3 - 1; *dx = (s - 34) % 3 - 1; }
+}
+
+// Gbar = a * (ZQ - ZQc) - 1/2 sum_c mu mu^T on the stencil (exact traces), or with
+// Hutchinson probes: a/nh1 * sym(Delta V^T) where Delta = TrQ - TrQc.
+__global__ void gbar_kernel(int Mx, int Ny, int T, int nslots, double a, const double* __restrict__ zq,
+                            const double* __restrict__ zqc, const double* __restrict__ dlt,
+                            const double* __restrict__ V, int nh1, const double* __restrict__ mu, int r,
+                            double* __restrict__ g) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t n = int64_t(Mx) * Ny * T;
+  if (e >= n * nslots) return;
+  const int k = int(e / nslots), s = int(e % nslots);
+  int dx, dy, dt;
+  slot_geo(T, s, &dx, &dy, &dt);
+  const int t = k / (Mx * Ny), c = k - t * Mx * Ny, y = c / Mx, x = c - y * Mx;
+  if (x + dx < 0 || x + dx >= Mx || y + dy < 0 || y + dy >= Ny || t + dt < 0 || t + dt >= T) {
+    g[e] = 0.0;
+    return;
+  }
+  const int64_t nb = (int64_t(t + dt) * Ny + y + dy) * Mx + x + dx;
+  double v = 0.0;
+  if (zq) {
+    v = a * (zq[e] - zqc[e]);
+  } else {
+    double acc = 0.0;
+    for (int p = 0; p < nh1; ++p)
+      acc += dlt[int64_t(k) * nh1 + p] * V[nb * nh1 + p] + dlt[nb * nh1 + p] * V[int64_t(k) * nh1 + p];
+    v = a * 0.5 * acc / nh1;
+  }
+  double mm = 0.0;
+  for (int cc = 0; cc < r; ++cc) mm += mu[int64_t(k) * r + cc] * mu[nb * r + cc];
+  g[e] = v - 0.5 * mm;
+}
+
+// sum over observations of z[idx_i, centre] (exact) or sum_p TrQc[idx_i,p] V[idx_i,p]
+__global__ void obs_trace_kernel(const int* __restrict__ idx, int m, const double* __restrict__ zqc, int nslots,
+                                 int centre, const double* __restrict__ trc, const double* __restrict__ V, int nh1,
+                                 double* __restrict__ part) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = blockIdx.x * 256 + threadIdx.x; i < m; i += gridDim.x * 256) {
+    const int64_t k = idx[i];
+    if (zqc) s += zqc[k * nslots + centre];
+    else
+      for (int p = 0; p < nh1; ++p) s += trc[k * nh1 + p] * V[k * nh1 + p];
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int q = 128; q > 0; q >>= 1) {
+    if (threadIdx.x < q) red[threadIdx.x] += red[threadIdx.x + q];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void sub_kernel(double* __restrict__ a, const double* __restrict__ b, int64_t n) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) a[i] -= b[i];
+}
+
+struct DevBuf {
+  double* p = nullptr;
+  size_t n = 0;
+  ~DevBuf() { cudaFree(p); }
+  cudaError_t ensure(size_t elems) {
+    if (elems <= n) return cudaSuccess;
+    cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, elems * sizeof(double));
+    if (e == cudaSuccess) n = elems;
+    return e;
+  }
+};
+
+double host_sum_partials(const double* dpart, int nblk, cudaStream_t st) {
+  std::vector<double> h(nblk);
+  cudaMemcpyAsync(h.data(), dpart, nblk * sizeof(double), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  double s = 0.0;
+  for (double v : h) s += v;
+  return s;
+}
+
+int ntheta_of(const Plan& p) { return 4 * p.model.nk + p.model.nw + 6; }
+
+}  // namespace
+
+struct LoglikeScratch {
+  DevBuf zq, zqc, b, mu, qmu, part, gbar, gradv, work, trq, trc, d;
+};
+
+struct SpdePlan {
+  Plan p;
+  LoglikeScratch s;
+};
+
+extern "C" {
+
+int spde_diffusion_triplets(int M, int N, const double* H, int field, double hx, double hy, int bc, int* row, int* col,
+                            double* val, void* stream) {
+  if (M < 1 || N < 1 || (bc != 1 && bc != 3) || !H || !row || !col || !val) return SPDE_ERR_ARG;
+  launch_diffusion_triplets(M, N, H, field, hx, hy, bc, row, col, val, static_cast<cudaStream_t>(stream));
+  return cudaGetLastError() == cudaSuccess ? SPDE_OK : SPDE_ERR_CUDA;
+}
+
+int spde_advection_triplets(int M, int N, const double* G, const double* dG, int field, double hx, double hy, int bc,
+                            int diff, int* row, int* col, double* val, void* stream) {
+  if (M < 1 || N < 1 || (bc != 1 && bc != 3) || diff < 1 || diff > 3 || !G || !row || !col || !val)
+    return SPDE_ERR_ARG;
+  launch_advection_triplets(M, N, G, dG, field, hx, hy, bc, diff, row, col, val, static_cast<cudaStream_t>(stream));
+  return cudaGetLastError() == cudaSuccess ? SPDE_OK : SPDE_ERR_CUDA;
+}
+
+static void fill_info(const Symbolic& S, SpdePlanInfo* info) {
+  info->n = S.n;
+  info->nfronts = int64_t(S.fronts.size());
+  info->max_depth = S.max_depth;
+  info->max_front = S.max_front;
+  info->nslots = S.nslots;
+  info->factor_flops = S.factor_flops;
+  info->selinv_flops = S.selinv_flops;
+  info->nnz_l = S.nnz_l;
+}
+
+int spde_symbolic_info(int Mx, int Ny, int T, int leaf_max, SpdePlanInfo* info) {
+  if (!info) return SPDE_ERR_ARG;
+  Symbolic S;
+  if (build_symbolic(Mx, Ny, T, leaf_max, 64, &S) != 0) return SPDE_ERR_ARG;
+  std::memset(info, 0, sizeof(*info));
+  fill_info(S, info);
+  info->precision = -1;
+  info->bytes_factor = double(S.l_size);
+  info->bytes_work = double(std::max(S.u_pool[0], S.z_pool[0]) + std::max(S.u_pool[1], S.z_pool[1]));
+  return SPDE_OK;
+}
+
+int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int32_t* front_ns, int32_t* front_nb,
+                         int32_t* front_parent, int64_t cap) {
+  Symbolic S;
+  if (build_symbolic(Mx, Ny, T, leaf_max, 64, &S) != 0) return SPDE_ERR_ARG;
+  if (perm) std::memcpy(perm, S.perm.data(), S.perm.size() * sizeof(int32_t));
+  if (int64_t(S.fronts.size()) > cap) return SPDE_ERR_ARG;
+  for (size_t f = 0; f < S.fronts.size(); ++f) {
+    if (front_ns) front_ns[f] = S.fronts[f].ns;
+    if (front_nb) front_nb[f] = S.fronts[f].nb;
+    if (front_parent) front_parent[f] = S.fronts[f].parent;
+  }
+  return SPDE_OK;
+}
+
+int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out) {
+  if (!out || (precision != 0 && precision != 1)) return SPDE_ERR_ARG;
+  *out = nullptr;
+  SpdePlan* plan = new (std::nothrow) SpdePlan();
+  if (!plan) return SPDE_ERR_NO_MEMORY;
+  plan->p.precision = precision;
+  if (build_symbolic(Mx, Ny, T, leaf_max > 0 ? leaf_max : 128, 64, &plan->p.sym) != 0) {
+    delete plan;
+    return SPDE_ERR_ARG;
+  }
+  int rc = plan_build(&plan->p);
+  if (rc != 0) {
+    spde_plan_destroy(plan);
+    return rc == 4 ? SPDE_ERR_NO_MEMORY : SPDE_ERR_CUDA;
+  }
+  *out = plan;
+  return SPDE_OK;
+}
+
+int spde_plan_destroy(SpdePlan* plan) {
+  if (!plan) return SPDE_OK;
+  Plan& p = plan->p;
+  cudaStreamSynchronize(p.stream);
+  void* ptrs[] = {p.d_fronts, p.d_perm, p.d_iperm, p.d_front_of, p.d_blist, p.d_rmap, p.d_amap, p.d_L, p.d_dinv,
+                  p.d_pool[0], p.d_pool[1], p.d_logpiv, p.d_err, p.d_scalar, p.d_bs, p.d_bsH, p.d_bsA, p.d_ww,
+                  p.d_theta, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.d_obs_cnt,
+                  p.d_obs_idx, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0], p.d_G[1], p.d_r, p.d_x64, p.d_b64};
+  for (void* q : ptrs) cudaFree(q);
+  p.sched_factor.release();
+  p.sched_selinv.release();
+  for (auto& kv : p.sched_fwd) kv.second->release();
+  for (auto& kv : p.sched_bwd) kv.second->release();
+  delete plan;
+  return SPDE_OK;
+}
+
+int spde_plan_set_stream(SpdePlan* plan, void* stream) {
+  if (!plan) return SPDE_ERR_ARG;
+  plan->p.stream = static_cast<cudaStream_t>(stream);
+  return SPDE_OK;
+}
+
+int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info) {
+  if (!plan || !info) return SPDE_ERR_ARG;
+  const Plan& p = plan->p;
+  std::memset(info, 0, sizeof(*info));
+  fill_info(p.sym, info);
+  info->precision = p.precision;
+  info->bytes_factor = double(p.sym.l_size) * p.esize();
+  info->bytes_work = double(p.pool_elems[0] + p.pool_elems[1]) * p.esize();
+  info->launches = p.launches_total;
+  return SPDE_OK;
+}
+
+const char* spde_last_error(const SpdePlan* plan) { return plan ? plan->p.last_error.c_str() : "null plan"; }
+
+int spde_set_model(SpdePlan* plan, const SpdeModelDesc* d) {
+  if (!plan || !d) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (d->Mx != p.sym.Mx || d->Ny != p.sym.Ny || d->T != p.sym.T) { p.last_error = "grid mismatch"; return SPDE_ERR_ARG; }
+  if ((d->bc != 1 && d->bc != 3) || d->diff_form < 0 || d->diff_form > 2 || d->adv < 0 || d->adv > 3) {
+    p.last_error = "unsupported model flags";
+    return SPDE_ERR_ARG;
+  }
+  if ((d->T == 1) != (d->adv == 0)) { p.last_error = "spatial models have no advection, spatio-temporal ones do"; return SPDE_ERR_ARG; }
+  const int Ns = d->Mx * d->Ny;
+  const int nb = std::max(d->nbasis, 1);
+  auto up = [&](double*& dst, const double* src, size_t n) -> int {
+    cudaFree(dst);
+    dst = nullptr;
+    if (!src) return 0;
+    if (cudaMalloc(&dst, n * sizeof(double)) != cudaSuccess) return 1;
+    return cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+  };
+  if ((d->var_h && (!d->bs || !d->bsH)) || (d->adv == 2 && !d->bsA) || (d->adv == 3 && !d->ww)) {
+    p.last_error = "missing basis or velocity field";
+    return SPDE_ERR_ARG;
+  }
+  if (up(p.d_bs, d->var_h ? d->bs : nullptr, size_t(Ns) * nb) || up(p.d_bsH, d->var_h ? d->bsH : nullptr, size_t(Ns) * 4 * nb) ||
+      up(p.d_bsA, d->adv == 2 ? d->bsA : nullptr, size_t(Ns) * 4 * nb) || up(p.d_ww, d->adv == 3 ? d->ww : nullptr, size_t(Ns) * 4)) {
+    p.last_error = "device allocation failed (model)";
+    return SPDE_ERR_NO_MEMORY;
+  }
+  DevModel& m = p.model;
+  m.Mx = d->Mx; m.Ny = d->Ny; m.T = d->T; m.Ns = Ns; m.bc = d->bc; m.mod0_bc = d->mod0_bc ? d->mod0_bc : d->bc;
+  m.hx = d->hx; m.hy = d->hy; m.dt = d->dt; m.V = d->hx * d->hy;
+  m.diff = d->diff_form; m.mod0_diff = d->mod0_diff_form; m.var_h = d->var_h; m.adv = d->adv; m.nbasis = nb;
+  m.nk = d->var_h ? nb : 1;
+  m.nw = d->adv == 1 ? 2 : d->adv == 2 ? 2 * nb : d->adv == 3 ? 1 : 0;
+  m.bs = p.d_bs; m.bsH = p.d_bsH; m.bsA = p.d_bsA; m.ww = p.d_ww;
+  double** arrs9[] = {&p.d_Ageo, &p.d_A0geo};
+  for (double** a : arrs9) { cudaFree(*a); API_CUDA(cudaMalloc(a, size_t(Ns) * 9 * sizeof(double))); }
+  double** arrs1[] = {&p.d_kap, &p.d_qs, &p.d_cQs};
+  for (double** a : arrs1) { cudaFree(*a); API_CUDA(cudaMalloc(a, size_t(Ns) * sizeof(double))); }
+  cudaFree(p.d_Q0); API_CUDA(cudaMalloc(&p.d_Q0, size_t(Ns) * 25 * sizeof(double)));
+  cudaFree(p.d_QA); API_CUDA(cudaMalloc(&p.d_QA, size_t(Ns) * 25 * sizeof(double)));
+  cudaFree(p.d_QO); API_CUDA(cudaMalloc(&p.d_QO, size_t(Ns) * 9 * sizeof(double)));
+  cudaFree(p.d_theta); API_CUDA(cudaMalloc(&p.d_theta, size_t(ntheta_of(p)) * sizeof(double)));
+  m.theta = p.d_theta;
+  p.model_set = true;
+  p.assembled = false;
+  p.factored = 0;
+  return SPDE_OK;
+}
+
+int spde_assemble(SpdePlan* plan, const double* theta, int ntheta) {
+  if (!plan || !theta) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.model_set) { p.last_error = "set a model first"; return SPDE_ERR_STATE; }
+  if (ntheta != ntheta_of(p)) { p.last_error = "theta length does not match the model"; return SPDE_ERR_ARG; }
+  for (int i = 0; i < ntheta; ++i)
+    if (!std::isfinite(theta[i])) { p.last_error = "non-finite parameter"; return SPDE_ERR_ARG; }
+  p.theta.assign(theta, theta + ntheta);
+  API_CUDA(cudaMemcpyAsync(p.d_theta, theta, ntheta * sizeof(double), cudaMemcpyHostToDevice, p.stream));
+  const double lsig = theta[4 * p.model.nk + p.model.nw];
+  p.cfac = p.sym.T > 1 ? 1.0 / (p.model.dt * std::exp(lsig)) : 1.0;
+  launch_fields(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.stream);
+  launch_qstencil(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.cfac, p.stream);
+  API_CUDA(cudaGetLastError());
+  p.assembled = true;
+  p.factored = 0;
+  return SPDE_OK;
+}
+
+int spde_export_q(SpdePlan* plan, int with_obs, double tau, double* q) {
+  if (!plan || !q) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  launch_qexport(p.qstencil(), p.sym.nslots, with_obs ? p.d_obs_cnt : nullptr, tau, q, p.stream);
+  API_CUDA(cudaGetLastError());
+  return SPDE_OK;
+}
+
+int spde_spmv(SpdePlan* plan, int with_obs, double tau, const double* x, double* y, int nrhs) {
+  if (!plan || !x || !y || nrhs < 1) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  launch_spmv(p.qstencil(), with_obs ? p.d_obs_cnt : nullptr, tau, x, y, nrhs, p.stream);
+  API_CUDA(cudaGetLastError());
+  return SPDE_OK;
+}
+
+int spde_set_obs(SpdePlan* plan, const int64_t* idx, int m) {
+  if (!plan || (m > 0 && !idx) || m < 0) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  std::vector<int> cnt(p.sym.n, 0), id(std::max(m, 1), 0);
+  for (int i = 0; i < m; ++i) {
+    if (idx[i] < 0 || idx[i] >= p.sym.n) { p.last_error = "observation index out of range"; return SPDE_ERR_ARG; }
+    cnt[idx[i]] += 1;
+    id[i] = int(idx[i]);
+  }
+  cudaFree(p.d_obs_cnt); cudaFree(p.d_obs_idx);
+  p.d_obs_cnt = nullptr; p.d_obs_idx = nullptr;
+  API_CUDA(cudaMalloc(&p.d_obs_cnt, cnt.size() * sizeof(int)));
+  API_CUDA(cudaMalloc(&p.d_obs_idx, id.size() * sizeof(int)));
+  API_CUDA(cudaMemcpy(p.d_obs_cnt, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice));
+  API_CUDA(cudaMemcpy(p.d_obs_idx, id.data(), id.size() * sizeof(int), cudaMemcpyHostToDevice));
+  p.nobs = m;
+  if (p.factored == 2) p.factored = 0;
+  return SPDE_OK;
+}
+
+int spde_factor(SpdePlan* plan, int with_obs, double tau, double* logdet) {
+  if (!plan) return SPDE_ERR_ARG;
+  int rc = plan_factor(&plan->p, with_obs, tau);
+  if (rc == 0 && logdet) *logdet = plan->p.logdet;
+  return rc;
+}
+
+int spde_solve(SpdePlan* plan, const double* b, double* x, int nrhs, int iters, double tol, double* resid) {
+  if (!plan || !b || !x) return SPDE_ERR_ARG;
+  return plan_solve(&plan->p, b, x, nrhs, iters, tol, resid);
+}
+
+int spde_sample(SpdePlan* plan, const double* z, double* x, int nrhs) {
+  if (!plan || !z || !x || nrhs < 1) return SPDE_ERR_ARG;
+  return plan_sample(&plan->p, z, x, nrhs);
+}
+
+int spde_selinv(SpdePlan* plan, double* zq) {
+  if (!plan || !zq) return SPDE_ERR_ARG;
+  return plan_selinv(&plan->p, zq);
+}
+
+int spde_adjoint(SpdePlan* plan, const double* gbar, double* grad_host) {
+  if (!plan || !gbar || !grad_host) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  const int nt = ntheta_of(p) - 1;
+  double *work = nullptr, *g = nullptr;
+  API_CUDA(cudaMalloc(&work, size_t(adjoint_work_elems(&p)) * sizeof(double)));
+  API_CUDA(cudaMalloc(&g, size_t(nt) * sizeof(double)));
+  launch_adjoint(&p, gbar, g, work, p.stream);
+  cudaError_t e = cudaMemcpyAsync(grad_host, g, nt * sizeof(double), cudaMemcpyDeviceToHost, p.stream);
+  cudaStreamSynchronize(p.stream);
+  cudaFree(work);
+  cudaFree(g);
+  if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) { p.last_error = "adjoint failed"; return SPDE_ERR_CUDA; }
+  return SPDE_OK;
+}
+
+int spde_conditional_mean(SpdePlan* plan, double tau, const double* y, const double* mu0, double* mu) {
+  if (!plan || !y || !mu) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.d_obs_idx) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  int rc = plan_factor(&p, 1, tau);
+  if (rc) return rc;
+  double* b = nullptr;
+  API_CUDA(cudaMalloc(&b, size_t(p.sym.n) * sizeof(double)));
+  API_CUDA(cudaMemsetAsync(b, 0, size_t(p.sym.n) * sizeof(double), p.stream));
+  obs_rhs_kernel<<<(p.nobs + 255) / 256 + 1, 256, 0, p.stream>>>(p.d_obs_idx, p.nobs, 1, tau, y, mu0, b);
+  double resid = 0.0;
+  rc = plan_solve(&p, b, mu, 1, p.precision == 0 ? 1 : 10, 1e-12, &resid);
+  if (rc == 0 && mu0) {
+    // mu += mu0, written as mu - (0 - mu0) with the subtraction kernel
+    API_CUDA(cudaMemsetAsync(b, 0, size_t(p.sym.n) * sizeof(double), p.stream));
+    sub_kernel<<<int((p.sym.n + 255) / 256), 256, 0, p.stream>>>(b, mu0, p.sym.n);
+    sub_kernel<<<int((p.sym.n + 255) / 256), 256, 0, p.stream>>>(mu, b, p.sym.n);
+  }
+  cudaStreamSynchronize(p.stream);
+  cudaFree(b);
+  return rc;
+}
+
+int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* y, int r, int grad_mode,
+                 const double* V, int nh1, double* f_out, double* jac) {
+  if (!plan || !theta || !y || r < 1 || !f_out || grad_mode < 0 || grad_mode > 2) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.d_obs_idx || p.nobs < 1) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  if (grad_mode == 2 && (!V || nh1 < 1)) { p.last_error = "Hutchinson mode needs probes"; return SPDE_ERR_ARG; }
+  if (grad_mode && !jac) return SPDE_ERR_ARG;
+  int rc = spde_assemble(plan, theta, ntheta);
+  if (rc) return rc;
+  cudaStream_t st = p.stream;
+  const int n = p.sym.n, ns = p.sym.nslots, m = p.nobs;
+  const double tau = std::exp(theta[ntheta - 1]);
+  LoglikeScratch& S = plan->s;
+  const int nblk = 256;
+  API_CUDA(S.part.ensure(nblk));
+  const bool exact = grad_mode == 1, hutch = grad_mode == 2;
+  if (exact) { API_CUDA(S.zq.ensure(size_t(n) * ns)); API_CUDA(S.zqc.ensure(size_t(n) * ns)); }
+  if (hutch) { API_CUDA(S.trq.ensure(size_t(n) * nh1)); API_CUDA(S.trc.ensure(size_t(n) * nh1)); }
+  const int iters = p.precision == 0 ? 1 : 10;
+  const double tol = 1e-12;
+  // Q: log-determinant, then its inverse on the pattern (or Hutchinson solves)
+  double ldq = 0.0, ldqc = 0.0, res = 0.0;
+  if ((rc = plan_factor(&p, 0, 0.0))) return rc;
+  ldq = p.logdet;
+  if (exact && (rc = plan_selinv(&p, S.zq.p))) return rc;
+  if (hutch && (rc = plan_solve(&p, V, S.trq.p, nh1, iters, tol, &res))) return rc;
+  // Q_c = Q + tau S^T S
+  if ((rc = plan_factor(&p, 1, tau))) return rc;
+  ldqc = p.logdet;
+  API_CUDA(S.b.ensure(size_t(n) * r));
+  API_CUDA(S.mu.ensure(size_t(n) * r));
+  API_CUDA(S.qmu.ensure(size_t(n) * r));
+  API_CUDA(S.d.ensure(size_t(m) * r));
+  API_CUDA(cudaMemsetAsync(S.b.p, 0, size_t(n) * r * sizeof(double), st));
+  obs_rhs_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, st>>>(p.d_obs_idx, m, r, tau, y, nullptr, S.b.p);
+  if ((rc = plan_solve(&p, S.b.p, S.mu.p, r, iters, tol, &res))) return rc;
+  if (hutch && (rc = plan_solve(&p, V, S.trc.p, nh1, iters, tol, &res))) return rc;
+  // quadratic terms
+  launch_spmv(p.qstencil(), nullptr, 0.0, S.mu.p, S.qmu.p, r, st);
+  dot_partial_kernel<<<nblk, 256, 0, st>>>(S.mu.p, S.qmu.p, int64_t(n) * r, S.part.p);
+  const double muqmu = host_sum_partials(S.part.p, nblk, st);
+  obs_resid_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, st>>>(p.d_obs_idx, m, r, y, S.mu.p, S.d.p);
+  dot_partial_kernel<<<nblk, 256, 0, st>>>(S.d.p, nullptr, int64_t(m) * r, S.part.p);
+  const double rss = host_sum_partials(S.part.p, nblk, st);
+  const double like = 0.5 * ldq * r + m * r * std::log(tau) / 2 - 0.5 * ldqc * r - 0.5 * muqmu - tau / 2 * rss;
+  *f_out = -like / (double(m) * r);
+  if (!grad_mode) return SPDE_OK;
+  if (exact && (rc = plan_selinv(&p, S.zqc.p))) return rc;
+  API_CUDA(S.gbar.ensure(size_t(n) * ns));
+  if (hutch) {
+    int64_t tot = int64_t(n) * nh1;
+    sub_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(S.trq.p, S.trc.p, tot);  // trq <- TrQ - TrQc
+  }
+  {
+    int64_t tot = int64_t(n) * ns;
+    gbar_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(p.sym.Mx, p.sym.Ny, p.sym.T, ns, 0.5 * r, exact ? S.zq.p : nullptr,
+                                                        S.zqc.p, S.trq.p, V, nh1, S.mu.p, r, S.gbar.p);
+  }
+  API_CUDA(S.work.ensure(size_t(adjoint_work_elems(&p))));
+  API_CUDA(S.gradv.ensure(size_t(ntheta)));
+  launch_adjoint(&p, S.gbar.p, S.gradv.p, S.work.p, st);
+  std::vector<double> g(ntheta, 0.0);
+  API_CUDA(cudaMemcpyAsync(g.data(), S.gradv.p, (ntheta - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+  const int centre = p.sym.T == 1 ? 12 : 21;
+  obs_trace_kernel<<<nblk, 256, 0, st>>>(p.d_obs_idx, m, exact ? S.zqc.p : nullptr, ns, centre, S.trc.p, V, nh1,
+                                         S.part.p);
+  const double tr = host_sum_partials(S.part.p, nblk, st);
+  API_CUDA(cudaGetLastError());
+  const double trace_term = exact ? tr : tr / nh1;
+  g[ntheta - 1] = m * r / 2.0 - 0.5 * r * tau * trace_term - tau / 2 * rss;
+  for (int i = 0; i < ntheta; ++i) jac[i] = -g[i] / (double(m) * r);
+  return SPDE_OK;
+}
+
+}  // extern "C"

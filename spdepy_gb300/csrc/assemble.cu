@@ -1,0 +1,360 @@
+// Q(theta) assembly: fields -> 9-point operator A -> compact per-cell stencils
+// of Q -> values scattered straight into the dense fronts of the factorisation.
+//
+// Reference path being replaced: makeQ (spdes/advection_diffusion2D.py:86-117,
+// spdes/var_advection_var_diffusion2D.py:83-116, spatial models e.g.
+// spdes/whittle_matern_anisotropic2D.py:59-75) with the stencils built by the
+// ccode/*.cpp libraries through ctypes and scipy sparse products.
+//
+// Because the coefficients are time-invariant (all interior time blocks are
+// identical), Q is held as four spatial stencils per cell (the first diagonal
+// block's 25 values, the interior diagonal block's 25, the off-diagonal 9 and the
+// kappa^2 diagonal), i.e. O(Ns) memory, and node values are formed on the fly.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "assemble.cuh"
+#include "stencil.cuh"
+
+namespace spde {
+
+__device__ __forceinline__ double dotb(const double* b, const double* c, int nb) {
+  double s = 0.0;
+  for (int i = 0; i < nb; ++i) s = fma(b[i], c[i], s);
+  return s;
+}
+
+// H = gamma I (iso), gamma I + v v^T (ani), or the half-angle form
+// gamma (cosh|v| I + sinh|v|/|v| [[vx, vy], [vy, -vx]]) (whittle_matern_ha2D.py:73-82);
+// out = {H00, H01, H10, H11}.  At |v| = 0 the half-angle ratio takes its limit 1.
+__device__ __forceinline__ void h_tensor(int diff, double g, double vx, double vy, double* out) {
+  if (diff == 0) {
+    out[0] = g; out[1] = 0.0; out[2] = 0.0; out[3] = g;
+  } else if (diff == 1) {
+    out[0] = g + vx * vx; out[1] = vx * vy; out[2] = vx * vy; out[3] = g + vy * vy;
+  } else {
+    double a = sqrt(vx * vx + vy * vy);
+    double ea = exp(a), eb = exp(-a);
+    double ch = (ea + eb) / 2, sh = (ea - eb) / 2;
+    double r = a > 0.0 ? sh / a : 1.0;
+    out[0] = g * (ch + r * vx); out[1] = g * r * vy; out[2] = g * r * vy; out[3] = g * (ch - r * vx);
+  }
+}
+
+// Field values of cell c (kappa, per-face H, per-face w) from the canonical theta.
+__device__ void cell_fields(const DevModel& m, int c, double* kappa, double* Hf /*16*/, double* wf /*4*/) {
+  const double* th = m.theta;
+  const int nk = m.nk, nb = m.nbasis;
+  if (m.var_h) {
+    *kappa = exp(dotb(m.bs + int64_t(c) * nb, th, nb));
+    for (int f = 0; f < 4; ++f) {
+      const double* b = m.bsH + (int64_t(c) * 4 + f) * nb;
+      double g = exp(dotb(b, th + nk, nb));
+      double vx = m.diff ? dotb(b, th + 2 * nk, nb) : 0.0;
+      double vy = m.diff ? dotb(b, th + 3 * nk, nb) : 0.0;
+      h_tensor(m.diff, g, vx, vy, Hf + 4 * f);
+    }
+  } else {
+    *kappa = exp(th[0]);
+    h_tensor(m.diff, exp(th[nk]), m.diff ? th[2 * nk] : 0.0, m.diff ? th[3 * nk] : 0.0, Hf);
+  }
+  const double* tw = th + 4 * nk;
+  if (m.adv == 1) {
+    wf[0] = tw[0]; wf[1] = tw[1];
+  } else if (m.adv == 2) {
+    for (int f = 0; f < 4; ++f) {
+      const double* b = m.bsA + (int64_t(c) * 4 + f) * nb;
+      wf[f] = dotb(b, tw + ((f & 1) ? nb : 0), nb);
+    }
+  } else if (m.adv == 3) {
+    for (int f = 0; f < 4; ++f) wf[f] = tw[0] * m.ww[int64_t(c) * 4 + f];
+  }
+}
+
+// A = V(1 + dt kappa) I - dt A_H + dt A_w (spatio-temporal) or V kappa I - A_H
+// (spatial), accumulated into the geometric 3x3 slots of each cell; A0 of the
+// initial-field model likewise.  Also Qs = V kappa^2.
+__global__ void fields_kernel(DevModel m, double* __restrict__ Ageo, double* __restrict__ A0geo,
+                              double* __restrict__ kap, double* __restrict__ qs) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.Ns) return;
+  const int M = m.Mx, N = m.Ny;
+  const int j = c / M, i = c - j * M;
+  double kappa, Hf[16], wf[4];
+  cell_fields(m, c, &kappa, Hf, wf);
+  double a[9];
+  for (int p = 0; p < 9; ++p) a[p] = 0.0;
+  const bool st = m.T > 1;
+  const double sc = st ? m.dt : 1.0;
+  a[4] = st ? m.V + m.V * kappa * m.dt : m.V * kappa;
+  double v[9];
+  int col[9];
+  bool keep[9];
+  CellH h = cell_h(Hf, m.var_h != 0, c, i, j, M, N, m.bc);
+  diffusion_cell(h, m.hx, m.hy, i, j, M, N, m.bc, v, col, keep);
+  for (int p = 0; p < 9; ++p)
+    if (keep[p]) a[geo9(col[p], i, j, M)] -= sc * v[p];
+  if (m.adv) {
+    advection_cell(wf, nullptr, m.adv != 1, m.hx, m.hy, i, j, M, N, m.bc, 3, v, col, keep);
+    for (int p = 0; p < 5; ++p)
+      if (keep[p]) a[geo9(col[p], i, j, M)] += m.dt * v[p];
+  }
+  for (int p = 0; p < 9; ++p) Ageo[int64_t(c) * 9 + p] = a[p];
+  kap[c] = kappa;
+  qs[c] = m.V * kappa * kappa;
+  if (st) {
+    const double* t0 = m.theta + 4 * m.nk + m.nw + 1;
+    double H0[4];
+    h_tensor(m.mod0_diff, exp(t0[1]), m.mod0_diff ? t0[2] : 0.0, m.mod0_diff ? t0[3] : 0.0, H0);
+    for (int p = 0; p < 9; ++p) a[p] = 0.0;
+    a[4] = m.V * exp(t0[0]);
+    CellH h0 = cell_h(H0, false, c, i, j, M, N, m.mod0_bc);
+    diffusion_cell(h0, m.hx, m.hy, i, j, M, N, m.mod0_bc, v, col, keep);
+    for (int p = 0; p < 9; ++p)
+      if (keep[p]) a[geo9(col[p], i, j, M)] -= v[p];
+    for (int p = 0; p < 9; ++p) A0geo[int64_t(c) * 9 + p] = a[p];
+  }
+}
+
+// (A^T D A)[k, k+d] over the 25 offsets d: sum over rows m of A in the 3x3
+// neighbourhood of k of A[m,k] D[m] A[m,l].
+__device__ void ata_row(const double* Ag, const double* D, double dscale, int c, int M, int N, double* out) {
+  for (int s = 0; s < 25; ++s) out[s] = 0.0;
+  const int j = c / M, i = c - j * M;
+  for (int dy1 = -1; dy1 <= 1; ++dy1)
+    for (int dx1 = -1; dx1 <= 1; ++dx1) {
+      // row m = k - (dx1, dy1); A[m, k] sits in slot (dx1, dy1) of row m
+      int mi = i - dx1, mj = j - dy1;
+      if (mi < 0 || mi >= M || mj < 0 || mj >= N) continue;
+      int mm = mj * M + mi;
+      const double* Am = Ag + int64_t(mm) * 9;
+      double amk = Am[(dy1 + 1) * 3 + (dx1 + 1)];
+      if (amk == 0.0) continue;
+      double w = amk * (D ? D[mm] * dscale : dscale);
+      for (int dy2 = -1; dy2 <= 1; ++dy2)
+        for (int dx2 = -1; dx2 <= 1; ++dx2) {
+          // column l = m + (dx2, dy2); offset from k = (dx2 - dx1, dy2 - dy1)
+          int ox = dx2 - dx1, oy = dy2 - dy1;
+          out[(oy + 2) * 5 + (ox + 2)] += w * Am[(dy2 + 1) * 3 + (dx2 + 1)];
+        }
+    }
+}
+
+__global__ void qstencil_kernel(DevModel m, const double* __restrict__ Ageo, const double* __restrict__ A0geo,
+                                const double* __restrict__ kap, const double* __restrict__ qs, double* __restrict__ Q0,
+                                double* __restrict__ QA, double* __restrict__ QO, double* __restrict__ cQs,
+                                double cfac) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.Ns) return;
+  double r[25];
+  if (m.T == 1) {
+    ata_row(Ageo, nullptr, 1.0 / m.V, c, m.Mx, m.Ny, r);
+    for (int s = 0; s < 25; ++s) QA[int64_t(c) * 25 + s] = r[s];
+    return;
+  }
+  // interior diagonal block: A^T (Qs / V^2) A, scaled by c = 1/(dt sigma)
+  // (spdes/advection_diffusion2D.py:103,112-116)
+  ata_row(Ageo, qs, 1.0 / (m.V * m.V), c, m.Mx, m.Ny, r);
+  for (int s = 0; s < 25; ++s) QA[int64_t(c) * 25 + s] = cfac * r[s];
+  ata_row(A0geo, nullptr, 1.0 / m.V, c, m.Mx, m.Ny, r);
+  for (int s = 0; s < 25; ++s) Q0[int64_t(c) * 25 + s] = r[s];
+  const double* Ac = Ageo + int64_t(c) * 9;
+  for (int p = 0; p < 9; ++p) QO[int64_t(c) * 9 + p] = -cfac * qs[c] / m.V * Ac[p];
+  cQs[c] = cfac * qs[c];
+}
+
+// Value of Q at node (cell c, time t), stencil offset (dx, dy, dt).
+__device__ __forceinline__ double qval(const QStencil& q, int c, int t, int dx, int dy, int dt) {
+  if (q.T == 1) return q.QA[int64_t(c) * 25 + (dy + 2) * 5 + dx + 2];
+  if (dt == 0) {
+    const int s = (dy + 2) * 5 + dx + 2;
+    const bool ctr = dx == 0 && dy == 0;
+    if (t == 0) return q.Q0[int64_t(c) * 25 + s] + (ctr ? q.cQs[c] : 0.0);
+    double v = q.QA[int64_t(c) * 25 + s];
+    if (t < q.T - 1 && ctr) v += q.cQs[c];
+    return v;
+  }
+  if (dt == 1) return q.QO[int64_t(c) * 9 + (dy + 1) * 3 + dx + 1];
+  const int mcell = c + dy * q.Mx + dx;
+  return q.QO[int64_t(mcell) * 9 + (1 - dy) * 3 + (1 - dx)];
+}
+
+__device__ __forceinline__ void slot_off(int T, int s, int* dx, int* dy, int* dt) {
+  if (T == 1) { *dt = 0; *dy = s / 5 - 2; *dx = s % 5 - 2; return; }
+  if (s < 9) { *dt = -1; *dy = s / 3 - 1; *dx = s % 3 - 1; }
+  else if (s < 34) { *dt = 0; *dy = (s - 9) / 5 - 2; *dx = (s - 9) % 5 - 2; }
+  else { *dt = 1; *dy = (s - 34) / 3 - 1; *dx = (s - 34) % 3 - 1; }
+}
+
+// Q in stencil layout (natural order, nslots values per node), FP64.
+__global__ void qexport_kernel(QStencil q, int nslots, const int* __restrict__ obs_cnt, double tau,
+                               double* __restrict__ out) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t n = int64_t(q.Ns) * q.T;
+  if (e >= n * nslots) return;
+  const int k = int(e / nslots), s = int(e % nslots);
+  const int t = k / q.Ns, c = k - t * q.Ns;
+  const int y = c / q.Mx, x = c - y * q.Mx;
+  int dx, dy, dt;
+  slot_off(q.T, s, &dx, &dy, &dt);
+  double v = 0.0;
+  if (x + dx >= 0 && x + dx < q.Mx && y + dy >= 0 && y + dy < q.Ny && t + dt >= 0 && t + dt < q.T) {
+    v = qval(q, c, t, dx, dy, dt);
+    if (obs_cnt && dx == 0 && dy == 0 && dt == 0) v += tau * obs_cnt[k];
+  }
+  out[e] = v;
+}
+
+// Scatter Q (or Q + tau S^T S) into the zeroed front panels.
+template <typename T>
+__global__ void scatter_kernel(QStencil q, int nslots, const int* __restrict__ amap, const int* __restrict__ perm,
+                               const int* __restrict__ front_of, const DevFront* __restrict__ fronts,
+                               const int* __restrict__ obs_cnt, double tau, T* __restrict__ L) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t n = int64_t(q.Ns) * q.T;
+  if (e >= n * nslots) return;
+  const int off = amap[e];
+  if (off < 0) return;
+  const int k = int(e / nslots), s = int(e % nslots);
+  const int t = k / q.Ns, c = k - t * q.Ns;
+  int dx, dy, dt;
+  slot_off(q.T, s, &dx, &dy, &dt);
+  double v = qval(q, c, t, dx, dy, dt);
+  if (obs_cnt && dx == 0 && dy == 0 && dt == 0) v += tau * obs_cnt[k];
+  const DevFront f = fronts[front_of[perm[k]]];
+  L[f.p_off + off] = T(v);
+}
+
+// y = (Q + tau S^T S) x for nrhs columns, natural order, FP64.
+__global__ void spmv_kernel(QStencil q, const int* __restrict__ obs_cnt, double tau, const double* __restrict__ x,
+                            double* __restrict__ y, int nrhs) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t n = int64_t(q.Ns) * q.T;
+  if (e >= n * nrhs) return;
+  const int k = int(e / nrhs), r = int(e % nrhs);
+  const int t = k / q.Ns, c = k - t * q.Ns;
+  const int yy = c / q.Mx, xx = c - yy * q.Mx;
+  const int ns = q.T == 1 ? 25 : 43;
+  double acc = 0.0;
+  for (int s = 0; s < ns; ++s) {
+    int dx, dy, dt;
+    slot_off(q.T, s, &dx, &dy, &dt);
+    int x2 = xx + dx, y2 = yy + dy, t2 = t + dt;
+    if (x2 < 0 || x2 >= q.Mx || y2 < 0 || y2 >= q.Ny || t2 < 0 || t2 >= q.T) continue;
+    int64_t nb = (int64_t(t2) * q.Ny + y2) * q.Mx + x2;
+    acc = fma(qval(q, c, t, dx, dy, dt), x[nb * nrhs + r], acc);
+  }
+  if (obs_cnt) acc = fma(tau * obs_cnt[k], x[int64_t(k) * nrhs + r], acc);
+  y[e] = acc;
+}
+
+// ---------------------------------------------------- stencil triplets (B3)
+__global__ void diffusion_triplet_kernel(int M, int N, const double* __restrict__ H, int field, double hx, double hy,
+                                         int bc, int* __restrict__ row, int* __restrict__ col,
+                                         double* __restrict__ val) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= M * N) return;
+  const int j = c / M, i = c - j * M;
+  CellH h = cell_h(field ? H + int64_t(c) * 16 : H, field != 0, c, i, j, M, N, bc);
+  double v[9];
+  int cl[9];
+  bool keep[9];
+  diffusion_cell(h, hx, hy, i, j, M, N, bc, v, cl, keep);
+  for (int p = 0; p < 9; ++p) {
+    row[int64_t(c) * 9 + p] = keep[p] ? c : M * N;
+    col[int64_t(c) * 9 + p] = cl[p];
+    val[int64_t(c) * 9 + p] = v[p];
+  }
+}
+
+__global__ void advection_triplet_kernel(int M, int N, const double* __restrict__ G, const double* __restrict__ dG,
+                                         int field, double hx, double hy, int bc, int diff, int* __restrict__ row,
+                                         int* __restrict__ col, double* __restrict__ val) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= M * N) return;
+  const int j = c / M, i = c - j * M;
+  double v[5];
+  int cl[5];
+  bool keep[5];
+  const double* g = field ? G + int64_t(c) * 4 : G;
+  const double* d = (field && dG) ? dG + int64_t(c) * 4 : nullptr;
+  advection_cell(g, d, field != 0, hx, hy, i, j, M, N, bc, diff, v, cl, keep);
+  for (int p = 0; p < 5; ++p) {
+    row[int64_t(c) * 5 + p] = keep[p] ? c : M * N;
+    col[int64_t(c) * 5 + p] = cl[p];
+    val[int64_t(c) * 5 + p] = v[p];
+  }
+}
+
+// ------------------------------------------------------------ permutations
+template <typename T>
+__global__ void to_new_kernel(const double* __restrict__ src, const int* __restrict__ perm, int n, int nrhs,
+                              T* __restrict__ dst) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(n) * nrhs) return;
+  const int k = int(e / nrhs), r = int(e % nrhs);
+  dst[int64_t(perm[k]) * nrhs + r] = T(src[e]);
+}
+
+template <typename T>
+__global__ void from_new_kernel(const T* __restrict__ src, const int* __restrict__ perm, int n, int nrhs,
+                                double* __restrict__ dst, int accumulate) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(n) * nrhs) return;
+  const int k = int(e / nrhs), r = int(e % nrhs);
+  double v = double(src[int64_t(perm[k]) * nrhs + r]);
+  dst[e] = accumulate ? dst[e] + v : v;
+}
+
+// ------------------------------------------------------------------ launchers
+static inline int nblk(int64_t n, int b) { return int((n + b - 1) / b); }
+
+void launch_fields(const DevModel& m, double* Ageo, double* A0geo, double* kap, double* qs, cudaStream_t st) {
+  fields_kernel<<<nblk(m.Ns, 128), 128, 0, st>>>(m, Ageo, A0geo, kap, qs);
+}
+void launch_qstencil(const DevModel& m, const double* Ageo, const double* A0geo, const double* kap, const double* qs,
+                     double* Q0, double* QA, double* QO, double* cQs, double cfac, cudaStream_t st) {
+  qstencil_kernel<<<nblk(m.Ns, 128), 128, 0, st>>>(m, Ageo, A0geo, kap, qs, Q0, QA, QO, cQs, cfac);
+}
+void launch_qexport(const QStencil& q, int nslots, const int* obs, double tau, double* out, cudaStream_t st) {
+  int64_t tot = int64_t(q.Ns) * q.T * nslots;
+  qexport_kernel<<<nblk(tot, 256), 256, 0, st>>>(q, nslots, obs, tau, out);
+}
+template <typename T>
+void launch_scatter(const QStencil& q, int nslots, const int* amap, const int* perm, const int* front_of,
+                    const DevFront* fronts, const int* obs, double tau, T* L, cudaStream_t st) {
+  int64_t tot = int64_t(q.Ns) * q.T * nslots;
+  scatter_kernel<T><<<nblk(tot, 256), 256, 0, st>>>(q, nslots, amap, perm, front_of, fronts, obs, tau, L);
+}
+template void launch_scatter<double>(const QStencil&, int, const int*, const int*, const int*, const DevFront*,
+                                     const int*, double, double*, cudaStream_t);
+template void launch_scatter<float>(const QStencil&, int, const int*, const int*, const int*, const DevFront*,
+                                    const int*, double, float*, cudaStream_t);
+void launch_spmv(const QStencil& q, const int* obs, double tau, const double* x, double* y, int nrhs,
+                 cudaStream_t st) {
+  int64_t tot = int64_t(q.Ns) * q.T * nrhs;
+  spmv_kernel<<<nblk(tot, 256), 256, 0, st>>>(q, obs, tau, x, y, nrhs);
+}
+void launch_diffusion_triplets(int M, int N, const double* H, int field, double hx, double hy, int bc, int* row,
+                               int* col, double* val, cudaStream_t st) {
+  diffusion_triplet_kernel<<<nblk(int64_t(M) * N, 128), 128, 0, st>>>(M, N, H, field, hx, hy, bc, row, col, val);
+}
+void launch_advection_triplets(int M, int N, const double* G, const double* dG, int field, double hx, double hy,
+                               int bc, int diff, int* row, int* col, double* val, cudaStream_t st) {
+  advection_triplet_kernel<<<nblk(int64_t(M) * N, 128), 128, 0, st>>>(M, N, G, dG, field, hx, hy, bc, diff, row,
+                                                                       col, val);
+}
+template <typename T>
+void launch_to_new(const double* src, const int* perm, int n, int nrhs, T* dst, cudaStream_t st) {
+  to_new_kernel<T><<<nblk(int64_t(n) * nrhs, 256), 256, 0, st>>>(src, perm, n, nrhs, dst);
+}
+template <typename T>
+void launch_from_new(const T* src, const int* perm, int n, int nrhs, double* dst, int acc, cudaStream_t st) {
+  from_new_kernel<T><<<nblk(int64_t(n) * nrhs, 256), 256, 0, st>>>(src, perm, n, nrhs, dst, acc);
+}
+template void launch_to_new<double>(const double*, const int*, int, int, double*, cudaStream_t);
+template void launch_to_new<float>(const double*, const int*, int, int, float*, cudaStream_t);
+template void launch_from_new<double>(const double*, const int*, int, int, double*, int, cudaStream_t);
+template void launch_from_new<float>(const float*, const int*, int, int, double*, int, cudaStream_t);
+
+}  // namespace spde

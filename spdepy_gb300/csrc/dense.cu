@@ -1,0 +1,248 @@
+// Batched dense kernels of the multifrontal factorisation, selected inversion
+// and solves.  Every launch walks a task list prepared once per lattice by the
+// symbolic phase, so fronts of very different sizes share one launch.
+//
+// This file holds the SIMT kernels (FP64 "plain" path, and the FP32 path on
+// tiles the tensor-core kernel does not take).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "kernels.cuh"
+
+namespace spde {
+
+// --------------------------------------------------------------------- GEMM
+template <typename T>
+struct GemmCfg;
+template <>
+struct GemmCfg<double> {
+  static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
+};
+template <>
+struct GemmCfg<float> {
+  static constexpr int BM = 128, BN = 128, BK = 16, TM = 8, TN = 8;
+};
+
+// A, B and C may alias (in-place triangular solves): every block reads all of
+// its A and B tiles before its epilogue writes C, and blocks own disjoint C tiles.
+template <typename T, int MODE, int AL, int BL>
+__global__ void __launch_bounds__(256) gemm_kernel(const GemmTask* __restrict__ tasks, const T* Ab, const T* Bb,
+                                                   T* Cb) {
+  using C = GemmCfg<T>;
+  constexpr int BM = C::BM, BN = C::BN, BK = C::BK, TM = C::TM, TN = C::TN;
+  __shared__ T As[BK][BM + 4];
+  __shared__ T Bs[BK][BN + 4];
+  const GemmTask tk = tasks[blockIdx.x];
+  const T* A = Ab + tk.a;
+  const T* B = Bb + tk.b;
+  T* Cp = Cb + tk.c;
+  const int tid = threadIdx.x;
+  const int tx = tid % (BN / TN);  // column group
+  const int ty = tid / (BN / TN);  // row group
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+  for (int k0 = 0; k0 < tk.k; k0 += BK) {
+    // A tile: BM x BK
+    for (int e = tid; e < BM * BK; e += 256) {
+      int i, kk;
+      if (AL == kRow) { kk = e % BK; i = e / BK; } else { i = e % BM; kk = e / BM; }
+      T v = T(0);
+      if (i < tk.m && k0 + kk < tk.k)
+        v = (AL == kRow) ? A[int64_t(i) * tk.lda + k0 + kk] : A[int64_t(k0 + kk) * tk.lda + i];
+      As[kk][i] = v;
+    }
+    for (int e = tid; e < BN * BK; e += 256) {
+      int j, kk;
+      if (BL == kRow) { kk = e % BK; j = e / BK; } else { j = e % BN; kk = e / BN; }
+      T v = T(0);
+      if (j < tk.n && k0 + kk < tk.k)
+        v = (BL == kRow) ? B[int64_t(j) * tk.ldb + k0 + kk] : B[int64_t(k0 + kk) * tk.ldb + j];
+      Bs[kk][j] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[kk][ty * TM + i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx * TN + j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    int r = ty * TM + i;
+    if (r >= tk.m) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      int c = tx * TN + j;
+      if (c >= tk.n) continue;
+      T* dst = Cp + int64_t(r) * tk.ldc + c;
+      if (MODE == kSub) *dst -= acc[i][j];
+      else if (MODE == kStore) *dst = acc[i][j];
+      else if (MODE == kNegStore) *dst = -acc[i][j];
+      else *dst += acc[i][j];
+    }
+  }
+}
+
+template <typename T, int MODE>
+static void gemm_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, int al, int bl, cudaStream_t st) {
+  if (al == kRow && bl == kRow) gemm_kernel<T, MODE, kRow, kRow><<<n, 256, 0, st>>>(t, A, B, C);
+  else if (al == kRow && bl == kCol) gemm_kernel<T, MODE, kRow, kCol><<<n, 256, 0, st>>>(t, A, B, C);
+  else if (al == kCol && bl == kRow) gemm_kernel<T, MODE, kCol, kRow><<<n, 256, 0, st>>>(t, A, B, C);
+  else gemm_kernel<T, MODE, kCol, kCol><<<n, 256, 0, st>>>(t, A, B, C);
+}
+
+template <typename T>
+void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout, int blayout,
+                 cudaStream_t st) {
+  if (ntasks <= 0) return;
+  switch (mode) {
+    case kSub: gemm_mode<T, kSub>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+    case kStore: gemm_mode<T, kStore>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+    case kNegStore: gemm_mode<T, kNegStore>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+    default: gemm_mode<T, kAdd>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+  }
+}
+
+template void launch_gemm<double>(const GemmTask*, int, const double*, const double*, double*, int, int, int,
+                                  cudaStream_t);
+template void launch_gemm<float>(const GemmTask*, int, const float*, const float*, float*, int, int, int,
+                                 cudaStream_t);
+
+// --------------------------------------------------- diagonal block POTRF
+// The block is factored in FP64 in shared memory whatever the storage type, so
+// the pivots (and the log-determinant) carry FP64 arithmetic.
+constexpr int kMaxNbk = 64;
+
+constexpr int kPotrfSmem = 2 * kMaxNbk * (kMaxNbk + 1) * sizeof(double);
+
+template <typename T>
+__global__ void __launch_bounds__(256) potrf_kernel(const DiagTask* __restrict__ tasks, T* __restrict__ L,
+                                                    T* __restrict__ dinv, double* __restrict__ logpiv,
+                                                    int* __restrict__ err) {
+  extern __shared__ double dsm[];
+  double(*a)[kMaxNbk + 1] = reinterpret_cast<double(*)[kMaxNbk + 1]>(dsm);
+  double(*x)[kMaxNbk + 1] = reinterpret_cast<double(*)[kMaxNbk + 1]>(dsm + kMaxNbk * (kMaxNbk + 1));
+  __shared__ double red[256];
+  __shared__ int bad;
+  const DiagTask tk = tasks[blockIdx.x];
+  const int w = tk.w;
+  const int tid = threadIdx.x;
+  T* blk = L + tk.a;
+  for (int e = tid; e < w * w; e += 256) {
+    int i = e / w, j = e % w;
+    a[i][j] = (j <= i) ? double(blk[int64_t(i) * tk.lda + j]) : 0.0;
+  }
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int j = 0; j < w; ++j) {
+    if (tid == 0) {
+      double d = a[j][j];
+      if (!(d > 0.0) || !isfinite(d)) { bad = 1; d = 1.0; }
+      a[j][j] = sqrt(d);
+    }
+    __syncthreads();
+    double piv = a[j][j];
+    for (int i = j + 1 + tid; i < w; i += 256) a[i][j] /= piv;
+    __syncthreads();
+    int rem = w - j - 1;
+    for (int e = tid; e < rem * rem; e += 256) {
+      int i = j + 1 + e / rem, k = j + 1 + e % rem;
+      if (k <= i) a[i][k] -= a[i][j] * a[k][j];
+    }
+    __syncthreads();
+  }
+  // inverse of the lower factor, one column per thread
+  for (int c = tid; c < w; c += 256) {
+    for (int i = 0; i < w; ++i) x[i][c] = 0.0;
+    x[c][c] = 1.0 / a[c][c];
+    for (int i = c + 1; i < w; ++i) {
+      double s = 0.0;
+      for (int k = c; k < i; ++k) s += a[i][k] * x[k][c];
+      x[i][c] = -s / a[i][i];
+    }
+  }
+  double lp = 0.0;
+  for (int j = tid; j < w; j += 256) lp += log(a[j][j]);
+  red[tid] = lp;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (tid < s) red[tid] += red[tid + s];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    logpiv[blockIdx.x] = red[0];
+    if (bad) atomicCAS(err, -1, tk.front);
+  }
+  T* dv = dinv + tk.dinv;
+  for (int e = tid; e < w * w; e += 256) {
+    int i = e / w, j = e % w;
+    blk[int64_t(i) * tk.lda + j] = T(j <= i ? a[i][j] : 0.0);
+    dv[int64_t(i) * kMaxNbk + j] = T(j <= i ? x[i][j] : 0.0);
+  }
+}
+
+template <typename T>
+void launch_potrf(const DiagTask* tasks, int ntasks, T* L, T* dinv, double* logpiv, int* err, cudaStream_t st) {
+  if (ntasks <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(potrf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPotrfSmem);
+    attr = true;
+  }
+  potrf_kernel<T><<<ntasks, 256, kPotrfSmem, st>>>(tasks, L, dinv, logpiv, err);
+}
+template void launch_potrf<double>(const DiagTask*, int, double*, double*, double*, int*, cudaStream_t);
+template void launch_potrf<float>(const DiagTask*, int, float*, float*, double*, int*, cudaStream_t);
+
+// ------------------------------------------------------------- extend-add
+// Adds the lower triangle of a child's update block into its parent's front:
+// columns inside the parent separator go to the parent panel P, the rest to the
+// parent's own update block U.  One launch per child rank, so no two blocks of
+// a launch touch the same parent entry.
+template <typename T>
+__global__ void __launch_bounds__(256) extend_add_kernel(const ExtendTask* __restrict__ tasks,
+                                                         const DevFront* __restrict__ fronts,
+                                                         const int* __restrict__ rmap, const T* __restrict__ Uc,
+                                                         T* __restrict__ L, T* __restrict__ Up) {
+  const ExtendTask tk = tasks[blockIdx.x];
+  const DevFront c = fronts[tk.child];
+  const DevFront p = fronts[c.parent];
+  const int* rm = rmap + c.b_off;
+  const T* U = Uc + c.u_off;
+  T* P = L + p.p_off;
+  T* Upar = Up + p.u_off;
+  for (int i = tk.r0; i < tk.r1; ++i) {
+    const int pi = rm[i];
+    const T* urow = U + int64_t(i) * c.ldu;
+    for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+      const int pj = rm[j];
+      const T v = urow[j];
+      if (pj < p.ns) P[int64_t(pi) * p.ld + pj] += v;
+      else Upar[int64_t(pi - p.ns) * p.ldu + (pj - p.ns)] += v;
+    }
+  }
+}
+
+template <typename T>
+void launch_extend_add(const ExtendTask* tasks, int ntasks, const DevFront* fronts, const int* rmap, const T* U_child,
+                       T* L, T* U_parent, cudaStream_t st) {
+  if (ntasks <= 0) return;
+  extend_add_kernel<T><<<ntasks, 256, 0, st>>>(tasks, fronts, rmap, U_child, L, U_parent);
+}
+template void launch_extend_add<double>(const ExtendTask*, int, const DevFront*, const int*, const double*, double*,
+                                        double*, cudaStream_t);
+template void launch_extend_add<float>(const ExtendTask*, int, const DevFront*, const int*, const float*, float*,
+                                       float*, cudaStream_t);
+
+}  // namespace spde

@@ -1,0 +1,884 @@
+// Numeric engine: launch schedules for the multifrontal factorisation, the
+// forward/backward solves and the Takahashi selected inversion, and their
+// execution on one stream.
+//
+// Replaces the CHOLMOD calls of the reference: cholesky(Q) + Factor.logdet()
+// (spdes/advection_diffusion2D.py:117,193,198), Factor.solve_A
+// (:194,201-202; model.py:126), Factor.solve_Lt + apply_Pt (model.py:80) and the
+// R-INLA selected inverse (model.py:89-118, rqinv.R:18-205).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+#include "engine.cuh"
+
+namespace spde {
+
+#define CUDA_TRY(x)                                                   \
+  do {                                                                \
+    cudaError_t e_ = (x);                                             \
+    if (e_ != cudaSuccess) {                                          \
+      p->last_error = std::string(#x) + ": " + cudaGetErrorString(e_); \
+      return 2;                                                       \
+    }                                                                 \
+  } while (0)
+
+constexpr int kNbk = 64;  // diagonal block size (kMaxNbk in dense.cu)
+
+// ----------------------------------------------------------- upload helpers
+template <typename X>
+static X* upload_vec(const std::vector<X>& v) {
+  if (v.empty()) return nullptr;
+  X* d = nullptr;
+  if (cudaMalloc(&d, v.size() * sizeof(X)) != cudaSuccess) return nullptr;
+  cudaMemcpy(d, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice);
+  return d;
+}
+
+void Schedule::upload() {
+  d_gemm = upload_vec(gemm);
+  d_diag = upload_vec(diag);
+  d_ext = upload_vec(ext);
+  d_rows = upload_vec(rows);
+  d_mirror = upload_vec(mirror);
+}
+void Schedule::release() {
+  cudaFree(d_gemm); cudaFree(d_diag); cudaFree(d_ext); cudaFree(d_rows); cudaFree(d_mirror);
+  d_gemm = nullptr; d_diag = nullptr; d_ext = nullptr; d_rows = nullptr; d_mirror = nullptr;
+}
+
+// ----------------------------------------------------------- schedule helpers
+struct Builder {
+  Schedule& s;
+  int TM, TN;
+  explicit Builder(Schedule& sc, int tm, int tn) : s(sc), TM(tm), TN(tn) {}
+
+  Op& begin(int kind) {
+    s.ops.push_back(Op());
+    Op& o = s.ops.back();
+    o.kind = kind;
+    switch (kind) {
+      case OP_GEMM: o.off = int64_t(s.gemm.size()); break;
+      case OP_DIAG: o.off = int64_t(s.diag.size()); break;
+      case OP_EXTEND: o.off = int64_t(s.ext.size()); break;
+      case OP_MIRROR: o.off = int64_t(s.mirror.size()); break;
+      default: o.off = int64_t(s.rows.size()); break;
+    }
+    return o;
+  }
+  void end() {
+    Op& o = s.ops.back();
+    switch (o.kind) {
+      case OP_GEMM: o.count = int(int64_t(s.gemm.size()) - o.off); break;
+      case OP_DIAG: o.count = int(int64_t(s.diag.size()) - o.off); break;
+      case OP_EXTEND: o.count = int(int64_t(s.ext.size()) - o.off); break;
+      case OP_MIRROR: o.count = int(int64_t(s.mirror.size()) - o.off); break;
+      case OP_MEMSET: o.count = 1; break;
+      default: o.count = int(int64_t(s.rows.size()) - o.off); break;
+    }
+    if (o.count == 0) s.ops.pop_back();
+    else ++s.launches;
+  }
+  // C[m x n] (op)= A B' tiled; A row i at a + i*arow_step, B row j at b + j*brow_step,
+  // C(i, j) at c + i*ldc + j.  lower: only tiles with row tile >= column tile.
+  void gemm_tiles(int64_t a, int lda, int64_t arow, int64_t b, int ldb, int64_t brow, int64_t c, int ldc, int m, int n,
+                  int k, bool lower = false, int i_start = 0) {
+    if (m <= 0 || n <= 0 || k <= 0) return;
+    for (int j0 = 0; j0 < n; j0 += TN)
+      for (int i0 = lower ? std::max(j0, i_start) : i_start; i0 < m; i0 += TM) {
+        GemmTask t;
+        t.a = a + int64_t(i0) * arow;
+        t.b = b + int64_t(j0) * brow;
+        t.c = c + int64_t(i0) * ldc + j0;
+        t.lda = lda; t.ldb = ldb; t.ldc = ldc;
+        t.m = std::min(TM, m - i0);
+        t.n = std::min(TN, n - j0);
+        t.k = k;
+        s.gemm.push_back(t);
+      }
+  }
+  void mirror_tiles(int64_t src, int64_t dst, int ld, int rows, int cols) {
+    for (int i0 = 0; i0 < rows; i0 += 32)
+      for (int j0 = 0; j0 < cols; j0 += 32) {
+        MirrorTask t;
+        t.src = src + int64_t(i0) * ld + j0;
+        t.dst = dst + int64_t(j0) * ld + i0;
+        t.ld = ld;
+        t.rows = std::min(32, rows - i0);
+        t.cols = std::min(32, cols - j0);
+        s.mirror.push_back(t);
+      }
+  }
+};
+
+static inline int nblocks(int ns) { return (ns + kNbk - 1) / kNbk; }
+
+static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int TN) {
+  Builder b(sc, TM, TN);
+  const auto& F = S.fronts;
+  for (int d = S.max_depth; d >= 0; --d) {
+    const auto& fr = S.by_depth[d];
+    const int pd = d & 1, pc = (d + 1) & 1;
+    // zero this depth's update blocks
+    int64_t used = 0;
+    for (int f : fr) used = std::max(used, F[f].u_off + int64_t(F[f].nb) * F[f].ldu);
+    if (used > 0) {
+      Op& o = b.begin(OP_MEMSET);
+      o.cbuf = pd == 0 ? B_P0 : B_P1;
+      o.elems = used;
+      b.end();
+    }
+    // extend-add of the children's update blocks, one launch per child rank
+    for (int rank = 0; rank < 2; ++rank) {
+      Op& o = b.begin(OP_EXTEND);
+      o.abuf = pc == 0 ? B_P0 : B_P1;
+      o.cbuf = pd == 0 ? B_P0 : B_P1;
+      o.depth = d;
+      for (int f : fr) {
+        int c = F[f].child[rank];
+        if (c < 0 || F[c].nb == 0) continue;
+        const int chunk = 8;
+        for (int r0 = 0; r0 < F[c].nb; r0 += chunk) sc.ext.push_back({c, r0, std::min(F[c].nb, r0 + chunk)});
+      }
+      b.end();
+    }
+    int steps = 0;
+    for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
+    for (int kb = 0; kb < steps; ++kb) {
+      Op& od = b.begin(OP_DIAG);
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk) continue;
+        DiagTask t;
+        t.w = std::min(kNbk, x.ns - kb * kNbk);
+        t.a = x.p_off + int64_t(kb) * kNbk * x.ld + kb * kNbk;
+        t.dinv = x.d_off + int64_t(kb) * kNbk * kNbk;
+        t.lda = x.ld;
+        t.front = f;
+        sc.diag.push_back(t);
+      }
+      b.end();
+      // panel below the diagonal block: X = A Linv^T (in place)
+      Op& ot = b.begin(OP_GEMM);
+      ot.mode = kStore; ot.al = kRow; ot.bl = kRow;
+      ot.abuf = B_L; ot.bbuf = B_DINV; ot.cbuf = B_L;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int r0 = kb * kNbk + w, rows = x.ns + x.nb - r0;
+        int64_t a = x.p_off + int64_t(r0) * x.ld + kb * kNbk;
+        b.gemm_tiles(a, x.ld, x.ld, x.d_off + int64_t(kb) * kNbk * kNbk, kNbk, kNbk, a, x.ld, rows, w, w);
+      }
+      b.end();
+      // trailing update of the panel's remaining separator columns
+      Op& ou = b.begin(OP_GEMM);
+      ou.mode = kSub; ou.al = kRow; ou.bl = kRow;
+      ou.abuf = B_L; ou.bbuf = B_L; ou.cbuf = B_L;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int c0 = kb * kNbk + w;
+        if (c0 >= x.ns) continue;
+        int rows = x.ns + x.nb - c0, cols = x.ns - c0;
+        int64_t a = x.p_off + int64_t(c0) * x.ld + kb * kNbk;
+        b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.p_off + int64_t(c0) * x.ld + c0, x.ld, rows, cols, w, true);
+      }
+      b.end();
+    }
+    // Schur complement of the rows below the separator: U -= P_B P_B^T
+    Op& os = b.begin(OP_GEMM);
+    os.mode = kSub; os.al = kRow; os.bl = kRow;
+    os.abuf = B_L; os.bbuf = B_L; os.cbuf = pd == 0 ? B_P0 : B_P1;
+    for (int f : fr) {
+      const Front& x = F[f];
+      if (x.nb == 0) continue;
+      int64_t a = x.p_off + int64_t(x.ns) * x.ld;
+      b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.u_off, x.ldu, x.nb, x.nb, x.ns, true);
+    }
+    b.end();
+  }
+}
+
+static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, int nrhs) {
+  Builder b(sc, TM, TN);
+  const auto& F = S.fronts;
+  const int chunk = std::max(1, std::min(nrhs, 16));
+  for (int d = S.max_depth; d >= 0; --d) {
+    const auto& fr = S.by_depth[d];
+    const int pd = d & 1;
+    Op& og = b.begin(OP_SGATHER_FWD);
+    og.depth = d;
+    for (int f : fr)
+      for (int r0 = 0; r0 < nrhs; r0 += chunk) sc.rows.push_back({f, r0, std::min(nrhs, r0 + chunk)});
+    b.end();
+    int steps = 0;
+    for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
+    for (int kb = 0; kb < steps; ++kb) {
+      Op& o1 = b.begin(OP_GEMM);  // y_k = Linv_k x_k (in place)
+      o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
+      o1.abuf = B_DINV; o1.bbuf = B_X; o1.cbuf = B_X;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int64_t xo = int64_t(x.s0 + kb * kNbk) * nrhs;
+        b.gemm_tiles(x.d_off + int64_t(kb) * kNbk * kNbk, kNbk, kNbk, xo, nrhs, 1, xo, nrhs, w, nrhs, w);
+      }
+      b.end();
+      Op& o2 = b.begin(OP_GEMM);  // x[S below] -= L y_k
+      o2.mode = kSub; o2.al = kRow; o2.bl = kCol;
+      o2.abuf = B_L; o2.bbuf = B_X; o2.cbuf = B_X;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int r0 = kb * kNbk + w;
+        int64_t xo = int64_t(x.s0 + kb * kNbk) * nrhs;
+        b.gemm_tiles(x.p_off + int64_t(r0) * x.ld + kb * kNbk, x.ld, x.ld, xo, nrhs, 1,
+                     int64_t(x.s0 + r0) * nrhs, nrhs, x.ns - r0, nrhs, w);
+      }
+      b.end();
+      Op& o3 = b.begin(OP_GEMM);  // W[B] -= L_B y_k
+      o3.mode = kSub; o3.al = kRow; o3.bl = kCol;
+      o3.abuf = B_L; o3.bbuf = B_X; o3.cbuf = pd == 0 ? B_W0 : B_W1;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk || x.nb == 0) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int64_t xo = int64_t(x.s0 + kb * kNbk) * nrhs;
+        b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld + kb * kNbk, x.ld, x.ld, xo, nrhs, 1, x.w_base * nrhs, nrhs,
+                     x.nb, nrhs, w);
+      }
+      b.end();
+    }
+  }
+}
+
+static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, int nrhs) {
+  Builder b(sc, TM, TN);
+  const auto& F = S.fronts;
+  const int chunk = std::max(1, std::min(nrhs, 16));
+  for (int d = 0; d <= S.max_depth; ++d) {
+    const auto& fr = S.by_depth[d];
+    const int pd = d & 1;
+    Op& og = b.begin(OP_SGATHER_BWD);
+    og.depth = d;
+    for (int f : fr)
+      if (F[f].nb > 0)
+        for (int r0 = 0; r0 < nrhs; r0 += chunk) sc.rows.push_back({f, r0, std::min(nrhs, r0 + chunk)});
+    b.end();
+    Op& o0 = b.begin(OP_GEMM);  // x_S -= L_BS^T x_B
+    o0.mode = kSub; o0.al = kCol; o0.bl = kCol;
+    o0.abuf = B_L; o0.bbuf = pd == 0 ? B_G0 : B_G1; o0.cbuf = B_X;
+    for (int f : fr) {
+      const Front& x = F[f];
+      if (x.nb == 0) continue;
+      b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld, x.ld, 1, x.w_base * nrhs, nrhs, 1, int64_t(x.s0) * nrhs, nrhs, x.ns,
+                   nrhs, x.nb);
+    }
+    b.end();
+    int steps = 0;
+    for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
+    for (int kb = steps - 1; kb >= 0; --kb) {
+      Op& o1 = b.begin(OP_GEMM);  // x_k = Linv_k^T x_k
+      o1.mode = kStore; o1.al = kCol; o1.bl = kCol;
+      o1.abuf = B_DINV; o1.bbuf = B_X; o1.cbuf = B_X;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int64_t xo = int64_t(x.s0 + kb * kNbk) * nrhs;
+        b.gemm_tiles(x.d_off + int64_t(kb) * kNbk * kNbk, kNbk, 1, xo, nrhs, 1, xo, nrhs, w, nrhs, w);
+      }
+      b.end();
+      if (kb == 0) continue;
+      Op& o2 = b.begin(OP_GEMM);  // x[rows above] -= L[k, rows]^T x_k
+      o2.mode = kSub; o2.al = kCol; o2.bl = kCol;
+      o2.abuf = B_L; o2.bbuf = B_X; o2.cbuf = B_X;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int64_t xo = int64_t(x.s0 + kb * kNbk) * nrhs;
+        b.gemm_tiles(x.p_off + int64_t(kb) * kNbk * x.ld, x.ld, 1, xo, nrhs, 1, int64_t(x.s0) * nrhs, nrhs, kb * kNbk,
+                     nrhs, w);
+      }
+      b.end();
+    }
+  }
+}
+
+static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int TN) {
+  Builder b(sc, TM, TN);
+  const auto& F = S.fronts;
+  for (int d = 0; d <= S.max_depth; ++d) {
+    const auto& fr = S.by_depth[d];
+    const int pz = d == 0 ? B_P0 : ((d & 1) == 0 ? B_P0 : B_P1);
+    {
+      Op& o = b.begin(OP_ZGATHER);
+      o.depth = d;
+      for (int f : fr) {
+        if (F[f].nb == 0) continue;
+        for (int r0 = 0; r0 < F[f].nb; r0 += 8) sc.rows.push_back({f, r0, std::min(F[f].nb, r0 + 8)});
+      }
+      b.end();
+    }
+    int steps = 0;
+    for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
+    // X = L_BS L_SS^-1, blocked right-looking from the last block column
+    for (int kb = steps - 1; kb >= 0; --kb) {
+      Op& o1 = b.begin(OP_GEMM);
+      o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
+      o1.abuf = B_L; o1.bbuf = B_DINV; o1.cbuf = B_L;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk || x.nb == 0) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        int64_t a = x.p_off + int64_t(x.ns) * x.ld + kb * kNbk;
+        b.gemm_tiles(a, x.ld, x.ld, x.d_off + int64_t(kb) * kNbk * kNbk, kNbk, 1, a, x.ld, x.nb, w, w);
+      }
+      b.end();
+      if (kb == 0) continue;
+      Op& o2 = b.begin(OP_GEMM);
+      o2.mode = kSub; o2.al = kRow; o2.bl = kCol;
+      o2.abuf = B_L; o2.bbuf = B_L; o2.cbuf = B_L;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= kb * kNbk || x.nb == 0) continue;
+        int w = std::min(kNbk, x.ns - kb * kNbk);
+        b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld + kb * kNbk, x.ld, x.ld, x.p_off + int64_t(kb) * kNbk * x.ld, x.ld,
+                     1, x.p_off + int64_t(x.ns) * x.ld, x.ld, x.nb, kb * kNbk, w);
+      }
+      b.end();
+    }
+    // Z_BS = -Z_BB X
+    {
+      Op& o = b.begin(OP_GEMM);
+      o.mode = kNegStore; o.al = kRow; o.bl = kCol;
+      o.abuf = pz; o.bbuf = B_L; o.cbuf = pz;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.nb == 0) continue;
+        b.gemm_tiles(x.z_off + int64_t(x.ns) * x.ldz + x.ns, x.ldz, x.ldz, x.p_off + int64_t(x.ns) * x.ld, x.ld, 1,
+                     x.z_off + int64_t(x.ns) * x.ldz, x.ldz, x.nb, x.ns, x.nb);
+      }
+      b.end();
+    }
+    // (L_SS L_SS^T)^-1 by the block-column Takahashi recursion, last block first
+    for (int J = steps - 1; J >= 0; --J) {
+      Op& ox = b.begin(OP_GEMM);  // X_J = L[R, J] Linv_J (in place)
+      ox.mode = kStore; ox.al = kRow; ox.bl = kCol;
+      ox.abuf = B_L; ox.bbuf = B_DINV; ox.cbuf = B_L;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= J * kNbk) continue;
+        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
+        if (nr <= 0) continue;
+        int64_t a = x.p_off + int64_t(R0) * x.ld + J * kNbk;
+        b.gemm_tiles(a, x.ld, x.ld, x.d_off + int64_t(J) * kNbk * kNbk, kNbk, 1, a, x.ld, nr, w, w);
+      }
+      b.end();
+      Op& oz = b.begin(OP_GEMM);  // Z[R, J] = -Z[R, R] X_J
+      oz.mode = kNegStore; oz.al = kRow; oz.bl = kCol;
+      oz.abuf = pz; oz.bbuf = B_L; oz.cbuf = pz;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= J * kNbk) continue;
+        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
+        if (nr <= 0) continue;
+        b.gemm_tiles(x.z_off + int64_t(R0) * x.ldz + R0, x.ldz, x.ldz, x.p_off + int64_t(R0) * x.ld + J * kNbk, x.ld, 1,
+                     x.z_off + int64_t(R0) * x.ldz + J * kNbk, x.ldz, nr, w, nr);
+      }
+      b.end();
+      Op& oj = b.begin(OP_GEMM);  // Z[J, J] = Linv_J^T Linv_J
+      oj.mode = kStore; oj.al = kCol; oj.bl = kCol;
+      oj.abuf = B_DINV; oj.bbuf = B_DINV; oj.cbuf = pz;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= J * kNbk) continue;
+        int w = std::min(kNbk, x.ns - J * kNbk);
+        int64_t dj = x.d_off + int64_t(J) * kNbk * kNbk;
+        b.gemm_tiles(dj, kNbk, 1, dj, kNbk, 1, x.z_off + int64_t(J) * kNbk * x.ldz + J * kNbk, x.ldz, w, w, w);
+      }
+      b.end();
+      Op& oj2 = b.begin(OP_GEMM);  // Z[J, J] -= X_J^T Z[R, J]
+      oj2.mode = kSub; oj2.al = kCol; oj2.bl = kCol;
+      oj2.abuf = B_L; oj2.bbuf = pz; oj2.cbuf = pz;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= J * kNbk) continue;
+        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
+        if (nr <= 0) continue;
+        b.gemm_tiles(x.p_off + int64_t(R0) * x.ld + J * kNbk, x.ld, 1, x.z_off + int64_t(R0) * x.ldz + J * kNbk,
+                     x.ldz, 1, x.z_off + int64_t(J) * kNbk * x.ldz + J * kNbk, x.ldz, w, w, nr);
+      }
+      b.end();
+      Op& om = b.begin(OP_MIRROR);  // Z[J, R] = Z[R, J]^T
+      om.cbuf = pz;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.ns <= J * kNbk) continue;
+        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
+        if (nr <= 0) continue;
+        b.mirror_tiles(x.z_off + int64_t(R0) * x.ldz + J * kNbk, x.z_off + int64_t(J) * kNbk * x.ldz + R0, x.ldz, nr,
+                       w);
+      }
+      b.end();
+    }
+    // Z_SS -= X^T Z_BS, then Z_SB = Z_BS^T
+    {
+      Op& o = b.begin(OP_GEMM);
+      o.mode = kSub; o.al = kCol; o.bl = kCol;
+      o.abuf = B_L; o.bbuf = pz; o.cbuf = pz;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.nb == 0) continue;
+        b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld, x.ld, 1, x.z_off + int64_t(x.ns) * x.ldz, x.ldz, 1, x.z_off, x.ldz,
+                     x.ns, x.ns, x.nb);
+      }
+      b.end();
+      Op& om = b.begin(OP_MIRROR);
+      om.cbuf = pz;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.nb == 0) continue;
+        b.mirror_tiles(x.z_off + int64_t(x.ns) * x.ldz, x.z_off + x.ns, x.ldz, x.nb, x.ns);
+      }
+      b.end();
+    }
+    {
+      Op& o = b.begin(OP_ZEXTRACT);
+      o.depth = d;
+      o.cbuf = pz;
+      for (int f : fr)
+        for (int r0 = 0; r0 < F[f].ns; r0 += 32) sc.rows.push_back({f, r0, std::min(F[f].ns, r0 + 32)});
+      b.end();
+    }
+  }
+}
+
+// ------------------------------------------------------------ small kernels
+template <typename T>
+__global__ void sgather_fwd_kernel(const RowTask* __restrict__ tasks, const DevFront* __restrict__ F,
+                                   const int* __restrict__ rmap, T* __restrict__ X, T* __restrict__ Wd,
+                                   const T* __restrict__ Wc, int nrhs) {
+  const RowTask tk = tasks[blockIdx.x];
+  const DevFront f = F[tk.front];
+  const int nr = tk.r1 - tk.r0;
+  T* W = Wd + f.w_base * nrhs;
+  for (int e = threadIdx.x; e < f.nb * nr; e += blockDim.x) W[int64_t(e / nr) * nrhs + tk.r0 + e % nr] = T(0);
+  __syncthreads();
+  for (int ci = 0; ci < 2; ++ci) {
+    if (f.child[ci] < 0) continue;
+    const DevFront c = F[f.child[ci]];
+    const int* rm = rmap + c.b_off;
+    const T* Wch = Wc + c.w_base * nrhs;
+    for (int e = threadIdx.x; e < c.nb * nr; e += blockDim.x) {
+      int bi = e / nr, r = tk.r0 + e % nr;
+      int pos = rm[bi];
+      T v = Wch[int64_t(bi) * nrhs + r];
+      if (pos < f.ns) X[int64_t(f.s0 + pos) * nrhs + r] += v;
+      else W[int64_t(pos - f.ns) * nrhs + r] += v;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void sgather_bwd_kernel(const RowTask* __restrict__ tasks, const DevFront* __restrict__ F,
+                                   const int* __restrict__ blist, const T* __restrict__ X, T* __restrict__ G,
+                                   int nrhs) {
+  const RowTask tk = tasks[blockIdx.x];
+  const DevFront f = F[tk.front];
+  const int nr = tk.r1 - tk.r0;
+  const int* bl = blist + f.b_off;
+  T* Gf = G + f.w_base * nrhs;
+  for (int e = threadIdx.x; e < f.nb * nr; e += blockDim.x) {
+    int bi = e / nr, r = tk.r0 + e % nr;
+    Gf[int64_t(bi) * nrhs + r] = X[int64_t(bl[bi]) * nrhs + r];
+  }
+}
+
+template <typename T>
+__global__ void zgather_kernel(const RowTask* __restrict__ tasks, const DevFront* __restrict__ F,
+                               const int* __restrict__ rmap, const T* __restrict__ Zp, T* __restrict__ Zc) {
+  const RowTask tk = tasks[blockIdx.x];
+  const DevFront f = F[tk.front];
+  const DevFront p = F[f.parent];
+  const int* rm = rmap + f.b_off;
+  for (int a = tk.r0; a < tk.r1; ++a) {
+    const T* src = Zp + p.z_off + int64_t(rm[a]) * p.ldz;
+    T* dst = Zc + f.z_off + int64_t(f.ns + a) * f.ldz + f.ns;
+    for (int bcol = threadIdx.x; bcol < f.nb; bcol += blockDim.x) dst[bcol] = src[rm[bcol]];
+  }
+}
+
+template <typename T>
+__global__ void mirror_kernel(const MirrorTask* __restrict__ tasks, T* __restrict__ Z) {
+  __shared__ T tile[32][33];
+  const MirrorTask tk = tasks[blockIdx.x];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int i = ty; i < 32; i += 8)
+    if (i < tk.rows && tx < tk.cols) tile[i][tx] = Z[tk.src + int64_t(i) * tk.ld + tx];
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8)
+    if (j < tk.cols && tx < tk.rows) Z[tk.dst + int64_t(j) * tk.ld + tx] = tile[tx][j];
+}
+
+template <typename T>
+__global__ void zextract_kernel(const RowTask* __restrict__ tasks, const DevFront* __restrict__ F,
+                                const int* __restrict__ iperm, const int* __restrict__ amap, int nslots,
+                                const T* __restrict__ Z, double* __restrict__ zq) {
+  const RowTask tk = tasks[blockIdx.x];
+  const DevFront f = F[tk.front];
+  const int cnt = (tk.r1 - tk.r0) * nslots;
+  for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+    int v = f.s0 + tk.r0 + e / nslots, s = e % nslots;
+    int k = iperm[v];
+    int off = amap[int64_t(k) * nslots + s];
+    if (off < 0) continue;
+    int row = off / f.ld, col = off - row * f.ld;
+    zq[int64_t(k) * nslots + s] = double(Z[f.z_off + int64_t(row) * f.ldz + col]);
+  }
+}
+
+__global__ void zsym_kernel(int Mx, int Ny, int T, int nslots, const int* __restrict__ amap, double* __restrict__ zq) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t n = int64_t(Mx) * Ny * T;
+  if (e >= n * nslots) return;
+  if (amap[e] >= 0) return;
+  const int k = int(e / nslots), s = int(e % nslots);
+  int dx, dy, dt;
+  if (T == 1) { dt = 0; dy = s / 5 - 2; dx = s % 5 - 2; }
+  else if (s < 9) { dt = -1; dy = s / 3 - 1; dx = s % 3 - 1; }
+  else if (s < 34) { dt = 0; dy = (s - 9) / 5 - 2; dx = (s - 9) % 5 - 2; }
+  else { dt = 1; dy = (s - 34) / 3 - 1; dx = (s - 34) % 3 - 1; }
+  const int t = k / (Mx * Ny), c = k - t * Mx * Ny, y = c / Mx, x = c - y * Mx;
+  if (x + dx < 0 || x + dx >= Mx || y + dy < 0 || y + dy >= Ny || t + dt < 0 || t + dt >= T) {
+    zq[e] = 0.0;
+    return;
+  }
+  const int64_t nb = (int64_t(t + dt) * Ny + y + dy) * Mx + x + dx;
+  const int opp = (T == 1 ? 24 : 42) - s;
+  zq[e] = zq[nb * nslots + opp];
+}
+
+__global__ void sum_kernel(const double* __restrict__ v, int64_t n, double* __restrict__ out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += 256) s += v[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// r = b - r (in place on r), and partial sums of |r|^2 and |b|^2
+__global__ void resid_kernel(const double* __restrict__ b, double* __restrict__ r, int64_t n,
+                             double* __restrict__ part) {
+  __shared__ double s1[256], s2[256];
+  double a1 = 0.0, a2 = 0.0;
+  for (int64_t i = int64_t(blockIdx.x) * 256 + threadIdx.x; i < n; i += int64_t(gridDim.x) * 256) {
+    double v = b[i] - r[i];
+    r[i] = v;
+    a1 += v * v;
+    a2 += b[i] * b[i];
+  }
+  s1[threadIdx.x] = a1;
+  s2[threadIdx.x] = a2;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) { s1[threadIdx.x] += s1[threadIdx.x + k]; s2[threadIdx.x] += s2[threadIdx.x + k]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { part[2 * blockIdx.x] = s1[0]; part[2 * blockIdx.x + 1] = s2[0]; }
+}
+
+// ------------------------------------------------------------------ executor
+template <typename T>
+struct Exec {
+  Plan* p;
+  const Schedule& s;
+  int nrhs;
+  double* zq;
+  T* buf(int id) const {
+    switch (id) {
+      case B_L: return static_cast<T*>(p->d_L);
+      case B_DINV: return static_cast<T*>(p->d_dinv);
+      case B_P0: return static_cast<T*>(p->d_pool[0]);
+      case B_P1: return static_cast<T*>(p->d_pool[1]);
+      case B_X: return static_cast<T*>(p->d_X);
+      case B_W0: return static_cast<T*>(p->d_W[0]);
+      case B_W1: return static_cast<T*>(p->d_W[1]);
+      case B_G0: return static_cast<T*>(p->d_G[0]);
+      case B_G1: return static_cast<T*>(p->d_G[1]);
+      default: return nullptr;
+    }
+  }
+  void run() {
+    cudaStream_t st = p->stream;
+    for (const Op& o : s.ops) {
+      switch (o.kind) {
+        case OP_MEMSET: cudaMemsetAsync(buf(o.cbuf), 0, size_t(o.elems) * sizeof(T), st); break;
+        case OP_EXTEND:
+          launch_extend_add<T>(s.d_ext + o.off, o.count, p->d_fronts, p->d_rmap, buf(o.abuf), buf(B_L), buf(o.cbuf),
+                               st);
+          break;
+        case OP_DIAG:
+          launch_potrf<T>(s.d_diag + o.off, o.count, buf(B_L), buf(B_DINV), p->d_logpiv + o.off, p->d_err, st);
+          break;
+        case OP_GEMM:
+          launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st);
+          break;
+        case OP_SGATHER_FWD: {
+          int pd = o.depth & 1;
+          sgather_fwd_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, p->d_rmap, buf(B_X),
+                                                         buf(pd ? B_W1 : B_W0), buf(pd ? B_W0 : B_W1), nrhs);
+          break;
+        }
+        case OP_SGATHER_BWD: {
+          int pd = o.depth & 1;
+          sgather_bwd_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, p->d_blist, buf(B_X),
+                                                         buf(pd ? B_G1 : B_G0), nrhs);
+          break;
+        }
+        case OP_ZGATHER: {
+          int pd = o.depth & 1;
+          zgather_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, p->d_rmap, buf(pd ? B_P0 : B_P1),
+                                                     buf(pd ? B_P1 : B_P0));
+          break;
+        }
+        case OP_MIRROR: mirror_kernel<T><<<o.count, 256, 0, st>>>(s.d_mirror + o.off, buf(o.cbuf)); break;
+        case OP_ZEXTRACT:
+          zextract_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, p->d_iperm, p->d_amap,
+                                                      p->sym.nslots, buf(o.cbuf), zq);
+          break;
+      }
+    }
+    p->launches_total += s.launches;
+  }
+};
+
+// ------------------------------------------------------------------- plan API
+int plan_build(Plan* p) {
+  Symbolic& S = p->sym;
+  const int TM = p->precision == 0 ? 64 : 128;
+  p->tile_m = TM;
+  p->tile_n = TM;
+  std::vector<DevFront> df(S.fronts.size());
+  p->w_elems_per_rhs[0] = std::max<int64_t>(S.w_pool[0], 1);
+  p->w_elems_per_rhs[1] = std::max<int64_t>(S.w_pool[1], 1);
+  for (size_t f = 0; f < S.fronts.size(); ++f) {
+    const Front& x = S.fronts[f];
+    DevFront& d = df[f];
+    d.p_off = x.p_off; d.u_off = x.u_off; d.z_off = x.z_off; d.b_off = x.b_off; d.d_off = x.d_off;
+    d.w_base = x.w_base;
+    d.s0 = x.s0; d.ns = x.ns; d.nb = x.nb; d.ld = x.ld; d.ldu = x.ldu; d.ldz = x.ldz;
+    d.parent = x.parent; d.depth = x.depth;
+    d.child[0] = x.child[0]; d.child[1] = x.child[1];
+  }
+  p->d_fronts = upload_vec(df);
+  p->d_perm = upload_vec(S.perm);
+  p->d_iperm = upload_vec(S.iperm);
+  p->d_front_of = upload_vec(S.front_of);
+  p->d_blist = upload_vec(S.blist);
+  p->d_rmap = upload_vec(S.rmap);
+  p->d_amap = upload_vec(S.amap);
+  if (!p->d_fronts || !p->d_perm || !p->d_amap) { p->last_error = "device allocation failed (symbolic)"; return 4; }
+  const size_t es = p->esize();
+  CUDA_TRY(cudaMalloc(&p->d_L, size_t(S.l_size) * es));
+  CUDA_TRY(cudaMalloc(&p->d_dinv, size_t(std::max<int64_t>(S.dinv_size, 1)) * es));
+  for (int k = 0; k < 2; ++k) {
+    p->pool_elems[k] = std::max<int64_t>(std::max(S.u_pool[k], S.z_pool[k]), 32);
+    CUDA_TRY(cudaMalloc(&p->d_pool[k], size_t(p->pool_elems[k]) * es));
+  }
+  build_factor_schedule(S, p->sched_factor, TM, TM);
+  build_selinv_schedule(S, p->sched_selinv, TM, TM);
+  p->sched_factor.upload();
+  p->sched_selinv.upload();
+  CUDA_TRY(cudaMalloc(&p->d_logpiv, std::max<size_t>(p->sched_factor.diag.size(), 1) * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&p->d_err, sizeof(int)));
+  CUDA_TRY(cudaMalloc(&p->d_scalar, 64 * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&p->d_part, 1024 * sizeof(double)));
+  return 0;
+}
+
+template <typename T>
+static int factor_t(Plan* p, int with_obs, double tau) {
+  const Symbolic& S = p->sym;
+  cudaStream_t st = p->stream;
+  CUDA_TRY(cudaMemsetAsync(p->d_L, 0, size_t(S.l_size) * sizeof(T), st));
+  int m1 = -1;
+  CUDA_TRY(cudaMemcpyAsync(p->d_err, &m1, sizeof(int), cudaMemcpyHostToDevice, st));
+  launch_scatter<T>(p->qstencil(), S.nslots, p->d_amap, p->d_perm, p->d_front_of, p->d_fronts,
+                    with_obs ? p->d_obs_cnt : nullptr, tau, static_cast<T*>(p->d_L), st);
+  Exec<T>{p, p->sched_factor, 0, nullptr}.run();
+  sum_kernel<<<1, 256, 0, st>>>(p->d_logpiv, int64_t(p->sched_factor.diag.size()), p->d_scalar);
+  double sum = 0.0;
+  int err = -1;
+  CUDA_TRY(cudaMemcpyAsync(&sum, p->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  CUDA_TRY(cudaGetLastError());
+  if (err >= 0) {
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "matrix is not positive definite (front %d)", err);
+    p->last_error = buf;
+    p->factored = 0;
+    return 3;
+  }
+  p->logdet = 2.0 * sum;
+  p->factored = with_obs ? 2 : 1;
+  p->factored_tau = tau;
+  return 0;
+}
+
+int plan_factor(Plan* p, int with_obs, double tau) {
+  if (!p->assembled) { p->last_error = "no assembled model"; return 5; }
+  if (with_obs && !p->d_obs_cnt) { p->last_error = "no observations set"; return 5; }
+  return p->precision == 0 ? factor_t<double>(p, with_obs, tau) : factor_t<float>(p, with_obs, tau);
+}
+
+static int ensure_solve_buffers(Plan* p, int nrhs) {
+  if (nrhs <= p->solve_cap) return 0;
+  const size_t es = p->esize();
+  cudaFree(p->d_X);
+  for (int k = 0; k < 2; ++k) { cudaFree(p->d_W[k]); cudaFree(p->d_G[k]); }
+  CUDA_TRY(cudaMalloc(&p->d_X, size_t(p->sym.n) * nrhs * es));
+  for (int k = 0; k < 2; ++k) {
+    CUDA_TRY(cudaMalloc(&p->d_W[k], size_t(p->w_elems_per_rhs[k]) * nrhs * es));
+    CUDA_TRY(cudaMalloc(&p->d_G[k], size_t(p->w_elems_per_rhs[k]) * nrhs * es));
+  }
+  p->solve_cap = nrhs;
+  return 0;
+}
+
+static int ensure_refine_buffers(Plan* p, int64_t elems) {
+  if (elems <= p->r_cap) return 0;
+  cudaFree(p->d_r); cudaFree(p->d_x64); cudaFree(p->d_b64);
+  CUDA_TRY(cudaMalloc(&p->d_r, size_t(elems) * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&p->d_x64, size_t(elems) * sizeof(double)));
+  CUDA_TRY(cudaMalloc(&p->d_b64, size_t(elems) * sizeof(double)));
+  p->r_cap = elems;
+  return 0;
+}
+
+template <typename T>
+static void tri_solve(Plan* p, int nrhs) {
+  auto& fw = p->sched_fwd[nrhs];
+  if (!fw) {
+    fw.reset(new Schedule());
+    build_fwd_schedule(p->sym, *fw, p->tile_m, p->tile_n, nrhs);
+    fw->upload();
+  }
+  auto& bw = p->sched_bwd[nrhs];
+  if (!bw) {
+    bw.reset(new Schedule());
+    build_bwd_schedule(p->sym, *bw, p->tile_m, p->tile_n, nrhs);
+    bw->upload();
+  }
+  Exec<T>{p, *fw, nrhs, nullptr}.run();
+  Exec<T>{p, *bw, nrhs, nullptr}.run();
+}
+
+template <typename T>
+static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, double tol, double* resid) {
+  const int n = p->sym.n;
+  const int64_t ne = int64_t(n) * nrhs;
+  cudaStream_t st = p->stream;
+  if (ensure_solve_buffers(p, nrhs)) return 2;
+  if (ensure_refine_buffers(p, ne)) return 2;
+  const int* obs = p->factored == 2 ? p->d_obs_cnt : nullptr;
+  const double tau = p->factored_tau;
+  // first solve straight from b
+  launch_to_new<T>(b, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);
+  tri_solve<T>(p, nrhs);
+  launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 0, st);
+  double rel = -1.0;
+  const int nblk = 512;
+  std::vector<double> part(2 * nblk);
+  for (int it = 0; it < iters; ++it) {
+    launch_spmv(p->qstencil(), obs, tau, x, p->d_r, nrhs, st);
+    resid_kernel<<<nblk, 256, 0, st>>>(b, p->d_r, ne, p->d_part);
+    CUDA_TRY(cudaMemcpyAsync(part.data(), p->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    double r2 = 0.0, b2 = 0.0;
+    for (int k = 0; k < nblk; ++k) { r2 += part[2 * k]; b2 += part[2 * k + 1]; }
+    rel = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    if (rel <= tol) break;
+    launch_to_new<T>(p->d_r, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);
+    tri_solve<T>(p, nrhs);
+    launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 1, st);
+  }
+  if (resid) {
+    if (rel < 0 || iters > 0) {
+      launch_spmv(p->qstencil(), obs, tau, x, p->d_r, nrhs, st);
+      resid_kernel<<<nblk, 256, 0, st>>>(b, p->d_r, ne, p->d_part);
+      CUDA_TRY(cudaMemcpyAsync(part.data(), p->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      double r2 = 0.0, b2 = 0.0;
+      for (int k = 0; k < nblk; ++k) { r2 += part[2 * k]; b2 += part[2 * k + 1]; }
+      rel = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    }
+    *resid = rel;
+  }
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+template <typename T>
+static int sample_t(Plan* p, const double* z, double* x, int nrhs) {
+  const int n = p->sym.n;
+  cudaStream_t st = p->stream;
+  if (ensure_solve_buffers(p, nrhs)) return 2;
+  auto& bw = p->sched_bwd[nrhs];
+  if (!bw) {
+    bw.reset(new Schedule());
+    build_bwd_schedule(p->sym, *bw, p->tile_m, p->tile_n, nrhs);
+    bw->upload();
+  }
+  launch_to_new<T>(z, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);
+  Exec<T>{p, *bw, nrhs, nullptr}.run();
+  launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 0, st);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int plan_sample(Plan* p, const double* z, double* x, int nrhs) {
+  if (!p->factored) { p->last_error = "no valid factor"; return 5; }
+  return p->precision == 0 ? sample_t<double>(p, z, x, nrhs) : sample_t<float>(p, z, x, nrhs);
+}
+
+int plan_solve(Plan* p, const double* b, double* x, int nrhs, int iters, double tol, double* resid) {
+  if (!p->factored) { p->last_error = "no valid factor (factor first; selinv consumes it)"; return 5; }
+  if (nrhs < 1) { p->last_error = "nrhs must be >= 1"; return 1; }
+  return p->precision == 0 ? solve_t<double>(p, b, x, nrhs, iters, tol, resid)
+                           : solve_t<float>(p, b, x, nrhs, iters, tol, resid);
+}
+
+template <typename T>
+static int selinv_t(Plan* p, double* zq) {
+  cudaStream_t st = p->stream;
+  const Symbolic& S = p->sym;
+  Exec<T>{p, p->sched_selinv, 0, zq}.run();
+  int64_t tot = int64_t(S.n) * S.nslots;
+  zsym_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(S.Mx, S.Ny, S.T, S.nslots, p->d_amap, zq);
+  CUDA_TRY(cudaGetLastError());
+  p->factored = 0;  // the factor's panels now hold intermediate products
+  return 0;
+}
+
+int plan_selinv(Plan* p, double* zq) {
+  if (!p->factored) { p->last_error = "no valid factor"; return 5; }
+  return p->precision == 0 ? selinv_t<double>(p, zq) : selinv_t<float>(p, zq);
+}
+
+}  // namespace spde

@@ -1,0 +1,129 @@
+// The plan: symbolic analysis, device arenas, precomputed launch schedules.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "assemble.cuh"
+#include "kernels.cuh"
+#include "spde_internal.h"
+
+namespace spde {
+
+enum OpKind {
+  OP_MEMSET = 0, OP_EXTEND, OP_DIAG, OP_GEMM, OP_SGATHER_FWD, OP_SGATHER_BWD, OP_ZGATHER, OP_MIRROR, OP_ZEXTRACT
+};
+enum BufId { B_NONE = 0, B_L, B_DINV, B_P0, B_P1, B_X, B_W0, B_W1, B_G0, B_G1 };
+
+struct Op {
+  int kind = 0;
+  int64_t off = 0;  // first task in the array of this kind
+  int count = 0;
+  int mode = 0, al = 0, bl = 0;
+  int abuf = B_NONE, bbuf = B_NONE, cbuf = B_NONE;
+  int64_t elems = 0;  // memset length
+  int depth = 0;
+};
+
+// Rectangle transpose: dst[j*ld + i] = src[i*ld + j], i < rows, j < cols (one 32x32 tile per task).
+struct MirrorTask {
+  int64_t src, dst;
+  int ld, rows, cols;
+};
+// Front-wide task over a row range (gathers, extraction).
+struct RowTask {
+  int front, r0, r1;
+};
+
+struct Schedule {
+  std::vector<Op> ops;
+  std::vector<GemmTask> gemm;
+  std::vector<DiagTask> diag;
+  std::vector<ExtendTask> ext;
+  std::vector<RowTask> rows;
+  std::vector<MirrorTask> mirror;
+  // device copies
+  GemmTask* d_gemm = nullptr;
+  DiagTask* d_diag = nullptr;
+  ExtendTask* d_ext = nullptr;
+  RowTask* d_rows = nullptr;
+  MirrorTask* d_mirror = nullptr;
+  int launches = 0;
+  void upload();
+  void release();
+};
+
+struct Plan {
+  Symbolic sym;
+  int precision = 1;  // 0: FP64 throughout ("plain"); 1: FP32 factor, FP64 pivots/refinement ("mixed")
+  int tile_m = 64, tile_n = 64;
+  cudaStream_t stream = nullptr;
+  // symbolic data on the device
+  DevFront* d_fronts = nullptr;
+  int *d_perm = nullptr, *d_iperm = nullptr, *d_front_of = nullptr, *d_blist = nullptr, *d_rmap = nullptr;
+  int* d_amap = nullptr;
+  // numeric arenas (element type = double for precision 0, float for 1)
+  void* d_L = nullptr;
+  void* d_dinv = nullptr;
+  void* d_pool[2] = {nullptr, nullptr};
+  int64_t pool_elems[2] = {0, 0};
+  double* d_logpiv = nullptr;
+  int* d_err = nullptr;
+  double* d_scalar = nullptr;  // small reduction outputs
+  double* d_part = nullptr;    // block partial sums (1024)
+  // model / assembly state (FP64)
+  DevModel model{};
+  bool model_set = false;
+  double *d_bs = nullptr, *d_bsH = nullptr, *d_bsA = nullptr, *d_ww = nullptr, *d_theta = nullptr;
+  double *d_Ageo = nullptr, *d_A0geo = nullptr, *d_kap = nullptr, *d_qs = nullptr;
+  double *d_Q0 = nullptr, *d_QA = nullptr, *d_QO = nullptr, *d_cQs = nullptr;
+  bool assembled = false;
+  double cfac = 1.0;
+  std::vector<double> theta;
+  // observations
+  int* d_obs_cnt = nullptr;   // per natural node
+  int* d_obs_idx = nullptr;   // observed natural nodes (m)
+  int nobs = 0;
+  // factor state
+  int factored = 0;  // 0 none, 1 Q, 2 Q + tau S^T S
+  double factored_tau = 0.0;
+  double logdet = 0.0;
+  // schedules
+  Schedule sched_factor, sched_selinv;
+  std::map<int, std::unique_ptr<Schedule>> sched_fwd, sched_bwd;
+  // solve buffers (sized for the largest nrhs seen)
+  int solve_cap = 0;
+  void* d_X = nullptr;
+  void* d_W[2] = {nullptr, nullptr};
+  void* d_G[2] = {nullptr, nullptr};
+  int64_t w_elems_per_rhs[2] = {0, 0};
+  double *d_r = nullptr, *d_x64 = nullptr, *d_b64 = nullptr;
+  int64_t r_cap = 0;
+  // counters
+  int64_t launches_total = 0;
+  std::string last_error;
+
+  QStencil qstencil() const {
+    QStencil q;
+    q.Q0 = d_Q0; q.QA = d_QA; q.QO = d_QO; q.cQs = d_cQs;
+    q.Mx = sym.Mx; q.Ny = sym.Ny; q.T = sym.T; q.Ns = sym.Mx * sym.Ny;
+    return q;
+  }
+  size_t esize() const { return precision == 0 ? sizeof(double) : sizeof(float); }
+};
+
+// engine entry points used by the C ABI
+int plan_build(Plan* p);
+int plan_factor(Plan* p, int with_obs, double tau);
+int plan_solve(Plan* p, const double* b_dev, double* x_dev, int nrhs, int refine_iters, double tol, double* resid);
+int plan_selinv(Plan* p, double* zq_dev);
+int plan_sample(Plan* p, const double* z_dev, double* x_dev, int nrhs);
+
+// adjoint (adjoint.cu)
+void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st);
+int64_t adjoint_work_elems(const Plan* p);
+
+}  // namespace spde

@@ -1,0 +1,55 @@
+// Kernel launch interfaces shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace spde {
+
+// One output tile of a batched product C (op)= A * B' over K.
+// A is addressed as A[i*lda + k] (arow) or A[k*lda + i] (acol);
+// B as B[j*ldb + k] (brow) or B[k*ldb + j] (bcol).  Offsets are in elements
+// relative to the base pointers passed at launch.
+struct GemmTask {
+  int64_t a, b, c;
+  int lda, ldb, ldc;
+  int m, n, k;
+};
+
+enum GemmMode { kSub = 0, kStore = 1, kNegStore = 2, kAdd = 3 };
+enum GemmLayout { kRow = 0, kCol = 1 };
+
+// Diagonal-block task: factor the w x w block at `a` (row stride lda) in place,
+// write its inverse to `dinv` (row stride nbk), record sum(log pivot).
+struct DiagTask {
+  int64_t a;
+  int64_t dinv;
+  int lda;
+  int w;
+  int front;
+};
+
+// Extend-add task: rows [r0, r1) of a child's update block.
+struct ExtendTask {
+  int child;
+  int r0, r1;
+};
+
+struct DevFront {
+  int64_t p_off, u_off, z_off, b_off, d_off;
+  int64_t w_base;  // offset (per right-hand side) of this front's solve vectors in its depth pool
+  int s0, ns, nb, ld, ldu, ldz, parent, depth;
+  int child[2];
+};
+
+template <typename T>
+void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout,
+                 int blayout, cudaStream_t st);
+
+template <typename T>
+void launch_potrf(const DiagTask* tasks, int ntasks, T* L, T* dinv, double* logpiv, int* err, cudaStream_t st);
+
+template <typename T>
+void launch_extend_add(const ExtendTask* tasks, int ntasks, const DevFront* fronts, const int* rmap, const T* U_child,
+                       T* L, T* U_parent, cudaStream_t st);
+
+}  // namespace spde
