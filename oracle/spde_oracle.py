@@ -411,7 +411,8 @@ class OracleModel:
         if self.fam.adv == "c":
             r, c, v = st.advection_const_triplets(g.Mx, g.Ny, w, g.hx, g.hy, self.bc, diff)
             return st.to_csc(g.Mx, g.Ny, r, c, v)
-        r, c, v = st.advection_field_triplets(g.Mx, g.Ny, w, g.hx, g.hy, self.bc, diff, dw)
+        safe = getattr(self, "derivative", "reference") == "true"
+        r, c, v = st.advection_field_triplets(g.Mx, g.Ny, w, g.hx, g.hy, self.bc, diff, dw, safe_sign=safe)
         return st.to_csc(g.Mx, g.Ny, r, c, v, nan_to_zero=(self.fam.adv == "v"))
 
     # ---------------------------------------------------------------- precision

@@ -188,13 +188,14 @@ def advection_const_triplets(M, N, G, hx, hy, bc, diff=3):
     return row.astype(np.int32).ravel(), col.astype(np.int32).ravel(), val.ravel()
 
 
-def advection_field_triplets(M, N, G, hx, hy, bc, diff=3, dG=None):
+def advection_field_triplets(M, N, G, hx, hy, bc, diff=3, dG=None, safe_sign=False):
     """5-point upwind advection for per-cell face velocities G (M*N, 4).
 
     Faces are ordered (E, N, W, S) = (0, 1, 2, 3) as in reference
     ``Aw_2D_b1.cpp:47-98``; bc=1 zeroes the boundary faces of the current cell in
     G and dG (on a copy here) before evaluating, bc=3 drops out-of-grid entries
-    (``Aw_2D_b3.cpp:37-81``).
+    (``Aw_2D_b3.cpp:37-81``).  ``safe_sign=True`` uses sign(G) (0 at G = 0) in
+    the derivative modes instead of the reference's G/|G| (NaN at 0).
     """
     i, j = _ij(M, N)
     n = M * N
@@ -230,7 +231,7 @@ def advection_field_triplets(M, N, G, hx, hy, bc, diff=3, dG=None):
         raise ValueError("bc must be 1 or 3")
     aG = np.abs(G)
     with np.errstate(invalid="ignore", divide="ignore"):
-        sG = G / aG
+        sG = np.sign(G) if safe_sign else G / aG
     if diff == 1:
         val = np.stack([(sG[:, 0] * dG[:, 0] + dG[:, 0] + sG[:, 2] * dG[:, 2] - dG[:, 2]) * hy / 2,
                         -(sG[:, 0] * dG[:, 0] - dG[:, 0]) * hy / 2,
