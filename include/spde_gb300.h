@@ -93,6 +93,13 @@ int spde_plan_destroy(SpdePlan* plan);
 int spde_plan_set_stream(SpdePlan* plan, void* stream);
 int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info);
 const char* spde_last_error(const SpdePlan* plan);
+/* Optional per-launch timing with CUDA events on the plan's stream (no
+ * reference counterpart; measurement only).  read_profile fills 9 entries per
+ * launch class (0 memset, 1 extend-add, 2 diagonal block, 3 tiled product,
+ * 4 forward gather, 5 backward gather, 6 inverse gather, 7 transpose,
+ * 8 inverse extraction): milliseconds, algorithmic flops, launches. */
+int spde_plan_set_profiling(SpdePlan* plan, int enable);
+int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* count, int reset);
 /* Symbolic analysis without a GPU (host only): statistics and the ordering. */
 int spde_symbolic_info(int Mx, int Ny, int T, int leaf_max, SpdePlanInfo* info);
 int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int32_t* front_ns, int32_t* front_nb,

@@ -243,6 +243,8 @@ int spde_plan_destroy(SpdePlan* plan) {
                   p.d_theta, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.d_obs_cnt,
                   p.d_obs_idx, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0], p.d_G[1], p.d_r, p.d_x64, p.d_b64};
   for (void* q : ptrs) cudaFree(q);
+  cudaFree(p.d_part);
+  for (cudaEvent_t e : p.ev_pool) cudaEventDestroy(e);
   p.sched_factor.release();
   p.sched_selinv.release();
   for (auto& kv : p.sched_fwd) kv.second->release();
@@ -270,6 +272,26 @@ int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info) {
 }
 
 const char* spde_last_error(const SpdePlan* plan) { return plan ? plan->p.last_error.c_str() : "null plan"; }
+
+int spde_plan_set_profiling(SpdePlan* plan, int enable) {
+  if (!plan) return SPDE_ERR_ARG;
+  prof_collect(&plan->p);
+  plan->p.profile = enable != 0;
+  return SPDE_OK;
+}
+
+int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* count, int reset) {
+  if (!plan) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  prof_collect(&p);
+  for (int k = 0; k < 9; ++k) {
+    if (ms) ms[k] = p.prof_ms[k];
+    if (flops) flops[k] = p.prof_flops[k];
+    if (count) count[k] = p.prof_count[k];
+    if (reset) { p.prof_ms[k] = 0; p.prof_flops[k] = 0; p.prof_count[k] = 0; }
+  }
+  return SPDE_OK;
+}
 
 int spde_set_model(SpdePlan* plan, const SpdeModelDesc* d) {
   if (!plan || !d) return SPDE_ERR_ARG;
@@ -333,6 +355,7 @@ int spde_assemble(SpdePlan* plan, const double* theta, int ntheta) {
   p.cfac = p.sym.T > 1 ? 1.0 / (p.model.dt * std::exp(lsig)) : 1.0;
   launch_fields(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.stream);
   launch_qstencil(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.cfac, p.stream);
+  p.launches_total += 2;
   API_CUDA(cudaGetLastError());
   p.assembled = true;
   p.factored = 0;
@@ -484,6 +507,7 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   obs_resid_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, st>>>(p.d_obs_idx, m, r, y, S.mu.p, S.d.p);
   dot_partial_kernel<<<nblk, 256, 0, st>>>(S.d.p, nullptr, int64_t(m) * r, S.part.p);
   const double rss = host_sum_partials(S.part.p, nblk, st);
+  p.launches_total += 5;  // obs rhs, spmv, two dot partials, obs residual
   const double like = 0.5 * ldq * r + m * r * std::log(tau) / 2 - 0.5 * ldqc * r - 0.5 * muqmu - tau / 2 * rss;
   *f_out = -like / (double(m) * r);
   if (!grad_mode) return SPDE_OK;
@@ -507,6 +531,7 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   obs_trace_kernel<<<nblk, 256, 0, st>>>(p.d_obs_idx, m, exact ? S.zqc.p : nullptr, ns, centre, S.trc.p, V, nh1,
                                          S.part.p);
   const double tr = host_sum_partials(S.part.p, nblk, st);
+  p.launches_total += 5 + (hutch ? 1 : 0);  // gbar, adjoint (3), obs trace, probe difference
   API_CUDA(cudaGetLastError());
   const double trace_term = exact ? tr : tr / nh1;
   g[ntheta - 1] = m * r / 2.0 - 0.5 * r * tau * trace_term - tau / 2 * rss;

@@ -98,6 +98,7 @@ struct Builder {
         t.n = std::min(TN, n - j0);
         t.k = k;
         s.gemm.push_back(t);
+        s.ops.back().flops += 2.0 * t.m * t.n * t.k;
       }
   }
   void mirror_tiles(int64_t src, int64_t dst, int ld, int rows, int cols) {
@@ -602,6 +603,38 @@ __global__ void resid_kernel(const double* __restrict__ b, double* __restrict__ 
   if (threadIdx.x == 0) { part[2 * blockIdx.x] = s1[0]; part[2 * blockIdx.x + 1] = s2[0]; }
 }
 
+// -------------------------------------------------------- per-launch timing
+static void prof_begin(Plan* p, cudaStream_t st) {
+  if (p->ev_used + 2 > p->ev_pool.size()) {
+    for (int i = 0; i < 512; ++i) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      p->ev_pool.push_back(e);
+    }
+  }
+  cudaEventRecord(p->ev_pool[p->ev_used], st);
+}
+static void prof_end(Plan* p, cudaStream_t st, int kind, double flops) {
+  cudaEventRecord(p->ev_pool[p->ev_used + 1], st);
+  p->ev_pending.push_back({kind, flops});
+  p->ev_used += 2;
+}
+// Fold the recorded event pairs into the per-kind totals (synchronises).
+void prof_collect(Plan* p) {
+  if (p->ev_pending.empty()) return;
+  cudaStreamSynchronize(p->stream);
+  for (size_t i = 0; i < p->ev_pending.size(); ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev_pool[2 * i], p->ev_pool[2 * i + 1]);
+    int k = p->ev_pending[i].first;
+    p->prof_ms[k] += ms;
+    p->prof_flops[k] += p->ev_pending[i].second;
+    p->prof_count[k] += 1;
+  }
+  p->ev_pending.clear();
+  p->ev_used = 0;
+}
+
 // ------------------------------------------------------------------ executor
 template <typename T>
 struct Exec {
@@ -626,6 +659,8 @@ struct Exec {
   void run() {
     cudaStream_t st = p->stream;
     for (const Op& o : s.ops) {
+      const bool timed = p->profile && o.kind != OP_MEMSET;
+      if (timed) prof_begin(p, st);
       switch (o.kind) {
         case OP_MEMSET: cudaMemsetAsync(buf(o.cbuf), 0, size_t(o.elems) * sizeof(T), st); break;
         case OP_EXTEND:
@@ -662,6 +697,7 @@ struct Exec {
                                                       p->sym.nslots, buf(o.cbuf), zq);
           break;
       }
+      if (timed) prof_end(p, st, o.kind, o.flops);
     }
     p->launches_total += s.launches;
   }
@@ -736,6 +772,8 @@ static int factor_t(Plan* p, int with_obs, double tau) {
     return 3;
   }
   p->logdet = 2.0 * sum;
+  p->launches_total += 2;  // scatter, log-pivot sum
+  if (p->profile) prof_collect(p);
   p->factored = with_obs ? 2 : 1;
   p->factored_tau = tau;
   return 0;
@@ -802,18 +840,21 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
   launch_to_new<T>(b, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);
   tri_solve<T>(p, nrhs);
   launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 0, st);
+  p->launches_total += 2;
   double rel = -1.0;
   const int nblk = 512;
   std::vector<double> part(2 * nblk);
   for (int it = 0; it < iters; ++it) {
     launch_spmv(p->qstencil(), obs, tau, x, p->d_r, nrhs, st);
     resid_kernel<<<nblk, 256, 0, st>>>(b, p->d_r, ne, p->d_part);
+    p->launches_total += 2;
     CUDA_TRY(cudaMemcpyAsync(part.data(), p->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     double r2 = 0.0, b2 = 0.0;
     for (int k = 0; k < nblk; ++k) { r2 += part[2 * k]; b2 += part[2 * k + 1]; }
     rel = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
     if (rel <= tol) break;
+    p->launches_total += 2;
     launch_to_new<T>(p->d_r, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);
     tri_solve<T>(p, nrhs);
     launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 1, st);
@@ -822,6 +863,7 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
     if (rel < 0 || iters > 0) {
       launch_spmv(p->qstencil(), obs, tau, x, p->d_r, nrhs, st);
       resid_kernel<<<nblk, 256, 0, st>>>(b, p->d_r, ne, p->d_part);
+      p->launches_total += 2;
       CUDA_TRY(cudaMemcpyAsync(part.data(), p->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
       CUDA_TRY(cudaStreamSynchronize(st));
       double r2 = 0.0, b2 = 0.0;
@@ -831,6 +873,7 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
     *resid = rel;
   }
   CUDA_TRY(cudaGetLastError());
+  if (p->profile) prof_collect(p);
   return 0;
 }
 
@@ -848,7 +891,9 @@ static int sample_t(Plan* p, const double* z, double* x, int nrhs) {
   launch_to_new<T>(z, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);
   Exec<T>{p, *bw, nrhs, nullptr}.run();
   launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 0, st);
+  p->launches_total += 2;
   CUDA_TRY(cudaGetLastError());
+  if (p->profile) prof_collect(p);
   return 0;
 }
 
@@ -871,7 +916,9 @@ static int selinv_t(Plan* p, double* zq) {
   Exec<T>{p, p->sched_selinv, 0, zq}.run();
   int64_t tot = int64_t(S.n) * S.nslots;
   zsym_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(S.Mx, S.Ny, S.T, S.nslots, p->d_amap, zq);
+  p->launches_total += 1;
   CUDA_TRY(cudaGetLastError());
+  if (p->profile) prof_collect(p);
   p->factored = 0;  // the factor's panels now hold intermediate products
   return 0;
 }

@@ -19,6 +19,7 @@ enum OpKind {
 enum BufId { B_NONE = 0, B_L, B_DINV, B_P0, B_P1, B_X, B_W0, B_W1, B_G0, B_G1 };
 
 struct Op {
+  double flops = 0.0;  // algorithmic flops of a GEMM launch (2 m n k summed over its tiles)
   int kind = 0;
   int64_t off = 0;  // first task in the array of this kind
   int count = 0;
@@ -102,8 +103,15 @@ struct Plan {
   int64_t w_elems_per_rhs[2] = {0, 0};
   double *d_r = nullptr, *d_x64 = nullptr, *d_b64 = nullptr;
   int64_t r_cap = 0;
-  // counters
+  // counters and optional per-launch timing (CUDA events on the plan's stream)
   int64_t launches_total = 0;
+  bool profile = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, double>> ev_pending;  // (op kind, flops) per recorded pair
+  size_t ev_used = 0;
+  double prof_ms[16] = {0};
+  double prof_flops[16] = {0};
+  int64_t prof_count[16] = {0};
   std::string last_error;
 
   QStencil qstencil() const {
@@ -121,6 +129,7 @@ int plan_factor(Plan* p, int with_obs, double tau);
 int plan_solve(Plan* p, const double* b_dev, double* x_dev, int nrhs, int refine_iters, double tol, double* resid);
 int plan_selinv(Plan* p, double* zq_dev);
 int plan_sample(Plan* p, const double* z_dev, double* x_dev, int nrhs);
+void prof_collect(Plan* p);
 
 // adjoint (adjoint.cu)
 void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st);
