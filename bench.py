@@ -186,6 +186,14 @@ def main():
     launches = plan.info().launches - launches0
     pms, pfl, pct = (np.zeros(9), np.zeros(9), np.zeros(9, dtype=np.int64))
     L.spde_plan_read_profile(plan.h, pms.ctypes.data, pfl.ctypes.data, pct.ctypes.data, 1)
+    sms, sfl, stl = np.zeros(18), np.zeros(18), np.zeros(18, dtype=np.int64)
+    L.spde_plan_read_sites(plan.h, sms.ctypes.data, sfl.ctypes.data, stl.ctypes.data, 1)
+    site_names = ["", "factor_panel_solve", "factor_panel_update", "factor_schur", "fwd_diag", "fwd_below", "fwd_border",
+                  "bwd_border", "bwd_diag", "bwd_above", "inv_x_solve", "inv_x_update", "inv_zbs", "inv_xj", "inv_zrj",
+                  "inv_zjj", "inv_zjj2", "inv_zss"]
+    sites = {site_names[i]: {"ms": round(float(sms[i] / args.steps), 3),
+                             "tflops": round(float(sfl[i] / max(sms[i], 1e-9) / 1e9), 2),
+                             "tiles": int(stl[i] // args.steps)} for i in range(1, 18) if sms[i] > 0}
     evals_per_s = world * args.steps / (ms / 1e3)
 
     # end to end through the public API: host data in, host objective/gradient out
@@ -255,6 +263,7 @@ def main():
              "transpose", "inv_extract"])},
         "algorithmic": {"factor_tflop": info.factor_flops / 1e12, "selinv_tflop": info.selinv_flops / 1e12,
                         "nnz_L": info.nnz_l},
+        "gemm_sites": sites,
         "objective": f, "clocks": clk, "cpu_baseline": cb, "fp64_plain": fp64,
     }
     print(json.dumps(line))

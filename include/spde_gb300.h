@@ -100,6 +100,9 @@ const char* spde_last_error(const SpdePlan* plan);
  * 8 inverse extraction): milliseconds, algorithmic flops, launches. */
 int spde_plan_set_profiling(SpdePlan* plan, int enable);
 int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* count, int reset);
+/* The same timing split by call site of the tiled product (18 entries: factor
+ * panel solve / panel update / Schur update, solve steps, inverse steps). */
+int spde_plan_read_sites(SpdePlan* plan, double* ms, double* flops, int64_t* tiles, int reset);
 /* Symbolic analysis without a GPU (host only): statistics and the ordering. */
 int spde_symbolic_info(int Mx, int Ny, int T, int leaf_max, SpdePlanInfo* info);
 int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int32_t* front_ns, int32_t* front_nb,

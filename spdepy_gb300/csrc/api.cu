@@ -280,6 +280,19 @@ int spde_plan_set_profiling(SpdePlan* plan, int enable) {
   return SPDE_OK;
 }
 
+int spde_plan_read_sites(SpdePlan* plan, double* ms, double* flops, int64_t* tiles, int reset) {
+  if (!plan) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  prof_collect(&p);
+  for (int k = 0; k < S_COUNT; ++k) {
+    if (ms) ms[k] = p.site_ms[k];
+    if (flops) flops[k] = p.site_flops[k];
+    if (tiles) tiles[k] = p.site_tiles[k];
+    if (reset) { p.site_ms[k] = 0; p.site_flops[k] = 0; p.site_tiles[k] = 0; }
+  }
+  return SPDE_OK;
+}
+
 int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* count, int reset) {
   if (!plan) return SPDE_ERR_ARG;
   Plan& p = plan->p;

@@ -6,6 +6,7 @@
 // tiles the tensor-core kernel does not take).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 
 #include "kernels.cuh"
 
@@ -102,10 +103,27 @@ static void gemm_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, in
   else gemm_kernel<T, MODE, kCol, kCol><<<n, 256, 0, st>>>(t, A, B, C);
 }
 
+// The FP32 products run on the tensor cores unless SPDE_TC=0 is set in the environment.
+bool tc_gemm_enabled() {
+  static int on = -1;
+  if (on < 0) {
+    const char* e = getenv("SPDE_TC");
+    on = (e && e[0] == '0') ? 0 : 1;
+  }
+  return on == 1;
+}
+
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout, int blayout,
-                 cudaStream_t st) {
+                 cudaStream_t st, bool tensor_cores) {
   if (ntasks <= 0) return;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (tensor_cores && tc_gemm_enabled()) {
+      launch_gemm_tc(tasks, ntasks, reinterpret_cast<const float*>(A), reinterpret_cast<const float*>(B),
+                     reinterpret_cast<float*>(C), mode, alayout, blayout, st);
+      return;
+    }
+  }
   switch (mode) {
     case kSub: gemm_mode<T, kSub>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
     case kStore: gemm_mode<T, kStore>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
@@ -115,9 +133,9 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
 }
 
 template void launch_gemm<double>(const GemmTask*, int, const double*, const double*, double*, int, int, int,
-                                  cudaStream_t);
+                                  cudaStream_t, bool);
 template void launch_gemm<float>(const GemmTask*, int, const float*, const float*, float*, int, int, int,
-                                 cudaStream_t);
+                                 cudaStream_t, bool);
 
 // --------------------------------------------------- diagonal block POTRF
 // The block is factored in FP64 in shared memory whatever the storage type, so

@@ -27,6 +27,7 @@ namespace spde {
   } while (0)
 
 constexpr int kNbk = 64;  // diagonal block size (kMaxNbk in dense.cu)
+constexpr int kTcMinK = 128;  // shortest K routed to the tensor-core product
 
 // ----------------------------------------------------------- upload helpers
 template <typename X>
@@ -70,7 +71,35 @@ struct Builder {
     return o;
   }
   void end() {
+    if (s.ops.back().kind == OP_GEMM) split_by_k();
+    finish(s.ops.back());
+  }
+  // Tiles with a short K (panel solves, rank-64 updates) run on the SIMT kernel,
+  // the others on the tensor-core kernel: split one GEMM launch into two, the
+  // first (already complete) and the second left for finish().
+  void split_by_k() {
     Op& o = s.ops.back();
+    const int64_t beg = o.off, end = int64_t(s.gemm.size());
+    auto mid = std::stable_partition(s.gemm.begin() + beg, s.gemm.begin() + end,
+                                     [](const GemmTask& t) { return t.k >= kTcMinK; });
+    const int64_t nlong = int64_t(mid - s.gemm.begin()) - beg;
+    if (nlong == 0 || beg + nlong == end) {
+      o.tc = nlong > 0 ? 1 : 0;
+      return;
+    }
+    Op second = o;
+    o.tc = 1;
+    o.flops = 0;
+    for (int64_t i = beg; i < beg + nlong; ++i) o.flops += 2.0 * s.gemm[i].m * s.gemm[i].n * s.gemm[i].k;
+    o.count = int(nlong);
+    ++s.launches;
+    second.off = beg + nlong;
+    second.tc = 0;
+    second.flops = 0;
+    for (int64_t i = beg + nlong; i < end; ++i) second.flops += 2.0 * s.gemm[i].m * s.gemm[i].n * s.gemm[i].k;
+    s.ops.push_back(second);
+  }
+  void finish(Op& o) {
     switch (o.kind) {
       case OP_GEMM: o.count = int(int64_t(s.gemm.size()) - o.off); break;
       case OP_DIAG: o.count = int(int64_t(s.diag.size()) - o.off); break;
@@ -164,7 +193,7 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       b.end();
       // panel below the diagonal block: X = A Linv^T (in place)
       Op& ot = b.begin(OP_GEMM);
-      ot.mode = kStore; ot.al = kRow; ot.bl = kRow;
+      ot.site = S_F_TRSM; ot.mode = kStore; ot.al = kRow; ot.bl = kRow;
       ot.abuf = B_L; ot.bbuf = B_DINV; ot.cbuf = B_L;
       for (int f : fr) {
         const Front& x = F[f];
@@ -177,7 +206,7 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       b.end();
       // trailing update of the panel's remaining separator columns
       Op& ou = b.begin(OP_GEMM);
-      ou.mode = kSub; ou.al = kRow; ou.bl = kRow;
+      ou.site = S_F_UPD; ou.mode = kSub; ou.al = kRow; ou.bl = kRow;
       ou.abuf = B_L; ou.bbuf = B_L; ou.cbuf = B_L;
       for (int f : fr) {
         const Front& x = F[f];
@@ -193,7 +222,7 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
     }
     // Schur complement of the rows below the separator: U -= P_B P_B^T
     Op& os = b.begin(OP_GEMM);
-    os.mode = kSub; os.al = kRow; os.bl = kRow;
+    os.site = S_F_SYRK; os.mode = kSub; os.al = kRow; os.bl = kRow;
     os.abuf = B_L; os.bbuf = B_L; os.cbuf = pd == 0 ? B_P0 : B_P1;
     for (int f : fr) {
       const Front& x = F[f];
@@ -221,7 +250,7 @@ static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
     for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
     for (int kb = 0; kb < steps; ++kb) {
       Op& o1 = b.begin(OP_GEMM);  // y_k = Linv_k x_k (in place)
-      o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
+      o1.site = S_V_FWD_D; o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
       o1.abuf = B_DINV; o1.bbuf = B_X; o1.cbuf = B_X;
       for (int f : fr) {
         const Front& x = F[f];
@@ -232,7 +261,7 @@ static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
       }
       b.end();
       Op& o2 = b.begin(OP_GEMM);  // x[S below] -= L y_k
-      o2.mode = kSub; o2.al = kRow; o2.bl = kCol;
+      o2.site = S_V_FWD_S; o2.mode = kSub; o2.al = kRow; o2.bl = kCol;
       o2.abuf = B_L; o2.bbuf = B_X; o2.cbuf = B_X;
       for (int f : fr) {
         const Front& x = F[f];
@@ -245,7 +274,7 @@ static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
       }
       b.end();
       Op& o3 = b.begin(OP_GEMM);  // W[B] -= L_B y_k
-      o3.mode = kSub; o3.al = kRow; o3.bl = kCol;
+      o3.site = S_V_FWD_B; o3.mode = kSub; o3.al = kRow; o3.bl = kCol;
       o3.abuf = B_L; o3.bbuf = B_X; o3.cbuf = pd == 0 ? B_W0 : B_W1;
       for (int f : fr) {
         const Front& x = F[f];
@@ -274,7 +303,7 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
         for (int r0 = 0; r0 < nrhs; r0 += chunk) sc.rows.push_back({f, r0, std::min(nrhs, r0 + chunk)});
     b.end();
     Op& o0 = b.begin(OP_GEMM);  // x_S -= L_BS^T x_B
-    o0.mode = kSub; o0.al = kCol; o0.bl = kCol;
+    o0.site = S_V_BWD_0; o0.mode = kSub; o0.al = kCol; o0.bl = kCol;
     o0.abuf = B_L; o0.bbuf = pd == 0 ? B_G0 : B_G1; o0.cbuf = B_X;
     for (int f : fr) {
       const Front& x = F[f];
@@ -287,7 +316,7 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
     for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
     for (int kb = steps - 1; kb >= 0; --kb) {
       Op& o1 = b.begin(OP_GEMM);  // x_k = Linv_k^T x_k
-      o1.mode = kStore; o1.al = kCol; o1.bl = kCol;
+      o1.site = S_V_BWD_D; o1.mode = kStore; o1.al = kCol; o1.bl = kCol;
       o1.abuf = B_DINV; o1.bbuf = B_X; o1.cbuf = B_X;
       for (int f : fr) {
         const Front& x = F[f];
@@ -299,7 +328,7 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
       b.end();
       if (kb == 0) continue;
       Op& o2 = b.begin(OP_GEMM);  // x[rows above] -= L[k, rows]^T x_k
-      o2.mode = kSub; o2.al = kCol; o2.bl = kCol;
+      o2.site = S_V_BWD_U; o2.mode = kSub; o2.al = kCol; o2.bl = kCol;
       o2.abuf = B_L; o2.bbuf = B_X; o2.cbuf = B_X;
       for (int f : fr) {
         const Front& x = F[f];
@@ -334,7 +363,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
     // X = L_BS L_SS^-1, blocked right-looking from the last block column
     for (int kb = steps - 1; kb >= 0; --kb) {
       Op& o1 = b.begin(OP_GEMM);
-      o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
+      o1.site = S_Z_XSOLVE; o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
       o1.abuf = B_L; o1.bbuf = B_DINV; o1.cbuf = B_L;
       for (int f : fr) {
         const Front& x = F[f];
@@ -346,7 +375,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       b.end();
       if (kb == 0) continue;
       Op& o2 = b.begin(OP_GEMM);
-      o2.mode = kSub; o2.al = kRow; o2.bl = kCol;
+      o2.site = S_Z_XUPD; o2.mode = kSub; o2.al = kRow; o2.bl = kCol;
       o2.abuf = B_L; o2.bbuf = B_L; o2.cbuf = B_L;
       for (int f : fr) {
         const Front& x = F[f];
@@ -360,7 +389,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
     // Z_BS = -Z_BB X
     {
       Op& o = b.begin(OP_GEMM);
-      o.mode = kNegStore; o.al = kRow; o.bl = kCol;
+      o.site = S_Z_BS; o.mode = kNegStore; o.al = kRow; o.bl = kCol;
       o.abuf = pz; o.bbuf = B_L; o.cbuf = pz;
       for (int f : fr) {
         const Front& x = F[f];
@@ -373,7 +402,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
     // (L_SS L_SS^T)^-1 by the block-column Takahashi recursion, last block first
     for (int J = steps - 1; J >= 0; --J) {
       Op& ox = b.begin(OP_GEMM);  // X_J = L[R, J] Linv_J (in place)
-      ox.mode = kStore; ox.al = kRow; ox.bl = kCol;
+      ox.site = S_Z_XJ; ox.mode = kStore; ox.al = kRow; ox.bl = kCol;
       ox.abuf = B_L; ox.bbuf = B_DINV; ox.cbuf = B_L;
       for (int f : fr) {
         const Front& x = F[f];
@@ -385,7 +414,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       }
       b.end();
       Op& oz = b.begin(OP_GEMM);  // Z[R, J] = -Z[R, R] X_J
-      oz.mode = kNegStore; oz.al = kRow; oz.bl = kCol;
+      oz.site = S_Z_RJ; oz.mode = kNegStore; oz.al = kRow; oz.bl = kCol;
       oz.abuf = pz; oz.bbuf = B_L; oz.cbuf = pz;
       for (int f : fr) {
         const Front& x = F[f];
@@ -397,7 +426,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       }
       b.end();
       Op& oj = b.begin(OP_GEMM);  // Z[J, J] = Linv_J^T Linv_J
-      oj.mode = kStore; oj.al = kCol; oj.bl = kCol;
+      oj.site = S_Z_JJ; oj.mode = kStore; oj.al = kCol; oj.bl = kCol;
       oj.abuf = B_DINV; oj.bbuf = B_DINV; oj.cbuf = pz;
       for (int f : fr) {
         const Front& x = F[f];
@@ -408,7 +437,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       }
       b.end();
       Op& oj2 = b.begin(OP_GEMM);  // Z[J, J] -= X_J^T Z[R, J]
-      oj2.mode = kSub; oj2.al = kCol; oj2.bl = kCol;
+      oj2.site = S_Z_JJ2; oj2.mode = kSub; oj2.al = kCol; oj2.bl = kCol;
       oj2.abuf = B_L; oj2.bbuf = pz; oj2.cbuf = pz;
       for (int f : fr) {
         const Front& x = F[f];
@@ -434,7 +463,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
     // Z_SS -= X^T Z_BS, then Z_SB = Z_BS^T
     {
       Op& o = b.begin(OP_GEMM);
-      o.mode = kSub; o.al = kCol; o.bl = kCol;
+      o.site = S_Z_SS; o.mode = kSub; o.al = kCol; o.bl = kCol;
       o.abuf = B_L; o.bbuf = pz; o.cbuf = pz;
       for (int f : fr) {
         const Front& x = F[f];
@@ -614,9 +643,10 @@ static void prof_begin(Plan* p, cudaStream_t st) {
   }
   cudaEventRecord(p->ev_pool[p->ev_used], st);
 }
-static void prof_end(Plan* p, cudaStream_t st, int kind, double flops) {
+static void prof_end(Plan* p, cudaStream_t st, int kind, double flops, int site, int tiles) {
   cudaEventRecord(p->ev_pool[p->ev_used + 1], st);
   p->ev_pending.push_back({kind, flops});
+  p->ev_site.push_back(site | (tiles << 8));
   p->ev_used += 2;
 }
 // Fold the recorded event pairs into the per-kind totals (synchronises).
@@ -630,8 +660,15 @@ void prof_collect(Plan* p) {
     p->prof_ms[k] += ms;
     p->prof_flops[k] += p->ev_pending[i].second;
     p->prof_count[k] += 1;
+    const int site = p->ev_site[i] & 255;
+    if (site > 0 && site < S_COUNT) {
+      p->site_ms[site] += ms;
+      p->site_flops[site] += p->ev_pending[i].second;
+      p->site_tiles[site] += p->ev_site[i] >> 8;
+    }
   }
   p->ev_pending.clear();
+  p->ev_site.clear();
   p->ev_used = 0;
 }
 
@@ -671,7 +708,8 @@ struct Exec {
           launch_potrf<T>(s.d_diag + o.off, o.count, buf(B_L), buf(B_DINV), p->d_logpiv + o.off, p->d_err, st);
           break;
         case OP_GEMM:
-          launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st);
+          launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st,
+                         o.tc != 0);
           break;
         case OP_SGATHER_FWD: {
           int pd = o.depth & 1;
@@ -697,7 +735,7 @@ struct Exec {
                                                       p->sym.nslots, buf(o.cbuf), zq);
           break;
       }
-      if (timed) prof_end(p, st, o.kind, o.flops);
+      if (timed) prof_end(p, st, o.kind, o.flops, o.site, o.kind == OP_GEMM ? o.count : 0);
     }
     p->launches_total += s.launches;
   }
@@ -764,6 +802,7 @@ static int factor_t(Plan* p, int with_obs, double tau) {
   CUDA_TRY(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   CUDA_TRY(cudaGetLastError());
+  if (tc_gemm_take_error()) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
   if (err >= 0) {
     char buf[128];
     std::snprintf(buf, sizeof(buf), "matrix is not positive definite (front %d)", err);
@@ -874,6 +913,7 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
   }
   CUDA_TRY(cudaGetLastError());
   if (p->profile) prof_collect(p);
+  if (tc_gemm_take_error()) { p->last_error = "tensor-core product timed out"; return 2; }
   return 0;
 }
 
@@ -917,7 +957,9 @@ static int selinv_t(Plan* p, double* zq) {
   int64_t tot = int64_t(S.n) * S.nslots;
   zsym_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(S.Mx, S.Ny, S.T, S.nslots, p->d_amap, zq);
   p->launches_total += 1;
+  CUDA_TRY(cudaStreamSynchronize(st));
   CUDA_TRY(cudaGetLastError());
+  if (tc_gemm_take_error()) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
   if (p->profile) prof_collect(p);
   p->factored = 0;  // the factor's panels now hold intermediate products
   return 0;

@@ -18,8 +18,16 @@ enum OpKind {
 };
 enum BufId { B_NONE = 0, B_L, B_DINV, B_P0, B_P1, B_X, B_W0, B_W1, B_G0, B_G1 };
 
+// Call sites of the tiled product (for per-site timing).
+enum GemmSite {
+  S_NONE = 0, S_F_TRSM, S_F_UPD, S_F_SYRK, S_V_FWD_D, S_V_FWD_S, S_V_FWD_B, S_V_BWD_0, S_V_BWD_D, S_V_BWD_U,
+  S_Z_XSOLVE, S_Z_XUPD, S_Z_BS, S_Z_XJ, S_Z_RJ, S_Z_JJ, S_Z_JJ2, S_Z_SS, S_COUNT
+};
+
 struct Op {
   double flops = 0.0;  // algorithmic flops of a GEMM launch (2 m n k summed over its tiles)
+  int site = 0;
+  int tc = 1;          // FP32 products: 1 = tensor-core kernel, 0 = SIMT kernel
   int kind = 0;
   int64_t off = 0;  // first task in the array of this kind
   int count = 0;
@@ -112,6 +120,10 @@ struct Plan {
   double prof_ms[16] = {0};
   double prof_flops[16] = {0};
   int64_t prof_count[16] = {0};
+  double site_ms[S_COUNT] = {0};
+  double site_flops[S_COUNT] = {0};
+  int64_t site_tiles[S_COUNT] = {0};
+  std::vector<int> ev_site;
   std::string last_error;
 
   QStencil qstencil() const {

@@ -43,7 +43,14 @@ struct DevFront {
 
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout,
-                 int blayout, cudaStream_t st);
+                 int blayout, cudaStream_t st, bool tensor_cores = true);
+
+// tcgen05 path for FP32 (tc_gemm.cu); tc_gemm_take_error returns and clears the
+// bounded-wait error flag of that kernel.
+void launch_gemm_tc(const GemmTask* tasks, int ntasks, const float* A, const float* B, float* C, int mode, int al,
+                    int bl, cudaStream_t st);
+int tc_gemm_take_error();
+bool tc_gemm_enabled();
 
 template <typename T>
 void launch_potrf(const DiagTask* tasks, int ntasks, T* L, T* dinv, double* logpiv, int* err, cudaStream_t st);
