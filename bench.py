@@ -220,6 +220,7 @@ def main():
     if args.fp64_steps > 0:
         m64 = build_model(w, "fp64")
         m64.initFit(w.y, idx=w.idx)
+        m64._ensure_model()
         m64.plan.set_obs(w.grid.obs_nodes(w.idx))
         c64 = m64.canonical(w.par)
         m64.plan.loglike(c64, y_dev, 1)

@@ -244,6 +244,7 @@ int spde_plan_destroy(SpdePlan* plan) {
                   p.d_obs_idx, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0], p.d_G[1], p.d_r, p.d_x64, p.d_b64};
   for (void* q : ptrs) cudaFree(q);
   cudaFree(p.d_part);
+  cudaFree(p.d_sx);
   for (cudaEvent_t e : p.ev_pool) cudaEventDestroy(e);
   p.sched_factor.release();
   p.sched_selinv.release();

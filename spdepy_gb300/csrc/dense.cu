@@ -142,16 +142,22 @@ template void launch_gemm<float>(const GemmTask*, int, const float*, const float
 // the pivots (and the log-determinant) carry FP64 arithmetic.
 constexpr int kMaxNbk = 64;
 
-constexpr int kPotrfSmem = 2 * kMaxNbk * (kMaxNbk + 1) * sizeof(double);
 
-template <typename T>
+// Arithmetic type A (FP64 on both paths; an FP32 sweep measured 1e-6 relative
+// log-likelihood error against 1e-7 for FP64 at 960k nodes).  The logs of the
+// pivots are taken in parallel after the sweep and summed in FP64.
+template <typename T, typename A>
 __global__ void __launch_bounds__(256) potrf_kernel(const DiagTask* __restrict__ tasks, T* __restrict__ L,
                                                     T* __restrict__ dinv, double* __restrict__ logpiv,
                                                     int* __restrict__ err) {
-  extern __shared__ double dsm[];
-  double(*a)[kMaxNbk + 1] = reinterpret_cast<double(*)[kMaxNbk + 1]>(dsm);
-  double(*x)[kMaxNbk + 1] = reinterpret_cast<double(*)[kMaxNbk + 1]>(dsm + kMaxNbk * (kMaxNbk + 1));
-  __shared__ double red[256];
+  // Right-looking Cholesky of the block and, in the same sweep, forward
+  // elimination of [L | I] for L^-1: after the pivot of column j, row j of the
+  // inverse is R_j / L_jj and every later row i drops L_ij times it.
+  extern __shared__ __align__(16) unsigned char dsm_raw[];
+  A* dsm = reinterpret_cast<A*>(dsm_raw);
+  A(*a)[kMaxNbk + 1] = reinterpret_cast<A(*)[kMaxNbk + 1]>(dsm);
+  A(*x)[kMaxNbk + 1] = reinterpret_cast<A(*)[kMaxNbk + 1]>(dsm + kMaxNbk * (kMaxNbk + 1));
+  __shared__ double lp[kMaxNbk];
   __shared__ int bad;
   const DiagTask tk = tasks[blockIdx.x];
   const int w = tk.w;
@@ -159,66 +165,69 @@ __global__ void __launch_bounds__(256) potrf_kernel(const DiagTask* __restrict__
   T* blk = L + tk.a;
   for (int e = tid; e < w * w; e += 256) {
     int i = e / w, j = e % w;
-    a[i][j] = (j <= i) ? double(blk[int64_t(i) * tk.lda + j]) : 0.0;
+    a[i][j] = (j <= i) ? A(blk[int64_t(i) * tk.lda + j]) : A(0);
+    x[i][j] = (i == j) ? A(1) : A(0);
   }
   if (tid == 0) bad = 0;
   __syncthreads();
   for (int j = 0; j < w; ++j) {
     if (tid == 0) {
-      double d = a[j][j];
-      if (!(d > 0.0) || !isfinite(d)) { bad = 1; d = 1.0; }
-      a[j][j] = sqrt(d);
+      A d = a[j][j];
+      if (!(d > A(0)) || !isfinite(double(d))) { bad = 1; d = A(1); }
+      const A piv = sqrt(d);
+      a[j][j] = piv;
+      lp[j] = double(piv);
     }
     __syncthreads();
-    double piv = a[j][j];
-    for (int i = j + 1 + tid; i < w; i += 256) a[i][j] /= piv;
+    const A inv = A(1) / a[j][j];
+    for (int e = tid; e < w; e += 256) {
+      if (e > j) a[e][j] *= inv;
+      if (e <= j) x[j][e] *= inv;
+    }
     __syncthreads();
-    int rem = w - j - 1;
-    for (int e = tid; e < rem * rem; e += 256) {
-      int i = j + 1 + e / rem, k = j + 1 + e % rem;
-      if (k <= i) a[i][k] -= a[i][j] * a[k][j];
+    const int rem = w - j - 1;
+    // a[i][k] -= a[i][j] a[k][j] (j < k <= i), x[i][c] -= a[i][j] x[j][c] (c <= j)
+    for (int e = tid; e < rem * (rem + j + 1); e += 256) {
+      const int i = j + 1 + e / (rem + j + 1), q = e % (rem + j + 1);
+      const A lij = a[i][j];
+      if (q < rem) {
+        const int k = j + 1 + q;
+        if (k <= i) a[i][k] -= lij * a[k][j];
+      } else {
+        const int c = q - rem;
+        x[i][c] -= lij * x[j][c];
+      }
     }
     __syncthreads();
   }
-  // inverse of the lower factor, one column per thread
-  for (int c = tid; c < w; c += 256) {
-    for (int i = 0; i < w; ++i) x[i][c] = 0.0;
-    x[c][c] = 1.0 / a[c][c];
-    for (int i = c + 1; i < w; ++i) {
-      double s = 0.0;
-      for (int k = c; k < i; ++k) s += a[i][k] * x[k][c];
-      x[i][c] = -s / a[i][i];
+  if (tid < 32) {
+    double s = 0.0;
+    for (int j = tid; j < w; j += 32) s += log(lp[j]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (tid == 0) {
+      logpiv[blockIdx.x] = s;
+      if (bad) atomicCAS(err, -1, tk.front);
     }
-  }
-  double lp = 0.0;
-  for (int j = tid; j < w; j += 256) lp += log(a[j][j]);
-  red[tid] = lp;
-  __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
-    if (tid < s) red[tid] += red[tid + s];
-    __syncthreads();
-  }
-  if (tid == 0) {
-    logpiv[blockIdx.x] = red[0];
-    if (bad) atomicCAS(err, -1, tk.front);
   }
   T* dv = dinv + tk.dinv;
   for (int e = tid; e < w * w; e += 256) {
     int i = e / w, j = e % w;
-    blk[int64_t(i) * tk.lda + j] = T(j <= i ? a[i][j] : 0.0);
-    dv[int64_t(i) * kMaxNbk + j] = T(j <= i ? x[i][j] : 0.0);
+    blk[int64_t(i) * tk.lda + j] = T(j <= i ? a[i][j] : A(0));
+    dv[int64_t(i) * kMaxNbk + j] = T(j <= i ? x[i][j] : A(0));
   }
 }
 
 template <typename T>
 void launch_potrf(const DiagTask* tasks, int ntasks, T* L, T* dinv, double* logpiv, int* err, cudaStream_t st) {
   if (ntasks <= 0) return;
+  using Arith = double;  // FP64 arithmetic on both paths (the mixed path's pivots carry the log-determinant)
+  const int smem = 2 * kMaxNbk * (kMaxNbk + 1) * int(sizeof(Arith));
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(potrf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPotrfSmem);
+    cudaFuncSetAttribute(potrf_kernel<T, Arith>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  potrf_kernel<T><<<ntasks, 256, kPotrfSmem, st>>>(tasks, L, dinv, logpiv, err);
+  potrf_kernel<T, Arith><<<ntasks, 256, smem, st>>>(tasks, L, dinv, logpiv, err);
 }
 template void launch_potrf<double>(const DiagTask*, int, double*, double*, double*, int*, cudaStream_t);
 template void launch_potrf<float>(const DiagTask*, int, float*, float*, double*, int*, cudaStream_t);

@@ -10,6 +10,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 
@@ -28,6 +29,8 @@ namespace spde {
 
 constexpr int kNbk = 64;  // diagonal block size (kMaxNbk in dense.cu)
 constexpr int kTcMinK = 128;  // shortest K routed to the tensor-core product
+enum { KT_NONE = 0, KT_A_UPPER, KT_B_LOWER, KT_BOTH_UPPER };
+constexpr int kPanel = 512;   // panel width of the two-level blocked factorisation
 
 // ----------------------------------------------------------- upload helpers
 template <typename X>
@@ -113,35 +116,47 @@ struct Builder {
   }
   // C[m x n] (op)= A B' tiled; A row i at a + i*arow_step, B row j at b + j*brow_step,
   // C(i, j) at c + i*ldc + j.  lower: only tiles with row tile >= column tile.
+  // kt: skip structurally zero K ranges of triangular row-layout operands whose
+  // K index shares the origin of their row index (KT_A_UPPER: A[i,k] = 0 for
+  // k < i; KT_B_LOWER: B[j,k] = 0 for k > j; KT_BOTH_UPPER: both upper).
   void gemm_tiles(int64_t a, int lda, int64_t arow, int64_t b, int ldb, int64_t brow, int64_t c, int ldc, int m, int n,
-                  int k, bool lower = false, int i_start = 0) {
+                  int k, bool lower = false, int i_start = 0, int kt = KT_NONE) {
     if (m <= 0 || n <= 0 || k <= 0) return;
     for (int j0 = 0; j0 < n; j0 += TN)
       for (int i0 = lower ? std::max(j0, i_start) : i_start; i0 < m; i0 += TM) {
+        int klo = 0, khi = k;
+        if (kt == KT_A_UPPER) klo = std::min(i0, k);
+        else if (kt == KT_B_LOWER) khi = std::min(k, j0 + TN);
+        else if (kt == KT_BOTH_UPPER) klo = std::min(std::max(i0, j0), k);
+        if (khi <= klo) { klo = 0; khi = std::min(k, 1); }
         GemmTask t;
-        t.a = a + int64_t(i0) * arow;
-        t.b = b + int64_t(j0) * brow;
+        t.a = a + int64_t(i0) * arow + klo;
+        t.b = b + int64_t(j0) * brow + klo;
         t.c = c + int64_t(i0) * ldc + j0;
         t.lda = lda; t.ldb = ldb; t.ldc = ldc;
         t.m = std::min(TM, m - i0);
         t.n = std::min(TN, n - j0);
-        t.k = k;
+        t.k = khi - klo;
         s.gemm.push_back(t);
         s.ops.back().flops += 2.0 * t.m * t.n * t.k;
       }
   }
-  void mirror_tiles(int64_t src, int64_t dst, int ld, int rows, int cols) {
+  // dst (ldd) <- src (lds), rows x cols of src, transposed or not, 32 x 32 per task
+  void copy_tiles(int64_t src, int lds, int64_t dst, int ldd, int rows, int cols, bool trans) {
     for (int i0 = 0; i0 < rows; i0 += 32)
       for (int j0 = 0; j0 < cols; j0 += 32) {
         MirrorTask t;
-        t.src = src + int64_t(i0) * ld + j0;
-        t.dst = dst + int64_t(j0) * ld + i0;
-        t.ld = ld;
+        t.src = src + int64_t(i0) * lds + j0;
+        t.dst = trans ? dst + int64_t(j0) * ldd + i0 : dst + int64_t(i0) * ldd + j0;
+        t.lds = lds;
+        t.ldd = ldd;
         t.rows = std::min(32, rows - i0);
         t.cols = std::min(32, cols - j0);
+        t.trans = trans ? 1 : 0;
         s.mirror.push_back(t);
       }
   }
+  void mirror_tiles(int64_t src, int64_t dst, int ld, int rows, int cols) { copy_tiles(src, ld, dst, ld, rows, cols, true); }
 };
 
 static inline int nblocks(int ns) { return (ns + kNbk - 1) / kNbk; }
@@ -204,7 +219,8 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         b.gemm_tiles(a, x.ld, x.ld, x.d_off + int64_t(kb) * kNbk * kNbk, kNbk, kNbk, a, x.ld, rows, w, w);
       }
       b.end();
-      // trailing update of the panel's remaining separator columns
+      // rank-64 update of the remaining columns of this 512-column panel
+      const int pstart = (kb * kNbk) / kPanel * kPanel, pend = pstart + kPanel;
       Op& ou = b.begin(OP_GEMM);
       ou.site = S_F_UPD; ou.mode = kSub; ou.al = kRow; ou.bl = kRow;
       ou.abuf = B_L; ou.bbuf = B_L; ou.cbuf = B_L;
@@ -212,13 +228,28 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         const Front& x = F[f];
         if (x.ns <= kb * kNbk) continue;
         int w = std::min(kNbk, x.ns - kb * kNbk);
-        int c0 = kb * kNbk + w;
-        if (c0 >= x.ns) continue;
-        int rows = x.ns + x.nb - c0, cols = x.ns - c0;
+        int c0 = kb * kNbk + w, c1 = std::min(x.ns, pend);
+        if (c0 >= c1) continue;
+        int rows = x.ns + x.nb - c0, cols = c1 - c0;
         int64_t a = x.p_off + int64_t(c0) * x.ld + kb * kNbk;
         b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.p_off + int64_t(c0) * x.ld + c0, x.ld, rows, cols, w, true);
       }
       b.end();
+      // at the end of a panel: one update of all later separator columns with K = panel width
+      if ((kb + 1) * kNbk == pend) {
+        Op& op = b.begin(OP_GEMM);
+        op.site = S_F_UPD; op.mode = kSub; op.al = kRow; op.bl = kRow;
+        op.abuf = B_L; op.bbuf = B_L; op.cbuf = B_L;
+        for (int f : fr) {
+          const Front& x = F[f];
+          if (x.ns <= pend) continue;
+          int rows = x.ns + x.nb - pend, cols = x.ns - pend;
+          int64_t a = x.p_off + int64_t(pend) * x.ld + pstart;
+          b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.p_off + int64_t(pend) * x.ld + pend, x.ld, rows, cols,
+                       kPanel, true);
+        }
+        b.end();
+      }
     }
     // Schur complement of the rows below the separator: U -= P_B P_B^T
     Op& os = b.begin(OP_GEMM);
@@ -343,12 +374,67 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
   }
 }
 
-static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int TN) {
+// Selected inversion, top-down over depths.  Per front (S = separator rows, B =
+// the rows below it, L = [L_SS; L_BS]), with Z_BB gathered from the parent:
+//   W   = L_SS^-1                 (recursive halving of the 64-blocks, below)
+//   X^T = W^T L_BS^T              (S x B)
+//   Z_SB = -X^T Z_BB,             Z_BS = Z_SB^T
+//   Z_SS = W^T W - X^T Z_SB^T     (lower tiles, then mirrored)
+// i.e. the Takahashi recursion Z_BS = -Z_BB L_BS L_SS^-1,
+// Z_SS = (L_SS L_SS^T)^-1 - (L_BS L_SS^-1)^T Z_BS, written so that every product
+// reads its operands row by row (K contiguous).  W and W^T are both kept
+// (row-major); for a node [a, b) of the halving tree with children [a, m), [m, b):
+//   TT = W_11^T L_21^T,  (W^T)_12 = -TT W_22^T,  W_21 = ((W^T)_12)^T.
+static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, int64_t* scratch_elems) {
   Builder b(sc, TM, TN);
   const auto& F = S.fronts;
+  auto r4 = [](int64_t v) { return (v + 3) / 4 * 4; };
+  int64_t scratch = 32;
   for (int d = 0; d <= S.max_depth; ++d) {
     const auto& fr = S.by_depth[d];
-    const int pz = d == 0 ? B_P0 : ((d & 1) == 0 ? B_P0 : B_P1);
+    const int pz = (d & 1) ? B_P1 : B_P0;
+    // scratch layout of this depth: W, W^T, X^T, TT per front
+    struct Sx { int64_t w, wt, xt, tt; int ldw, ldx; std::vector<std::vector<std::array<int, 3>>> levels; };
+    std::vector<Sx> sx(fr.size());
+    int64_t off = 0;
+    int maxlev = 0;
+    for (size_t q = 0; q < fr.size(); ++q) {
+      const Front& x = F[fr[q]];
+      Sx& z = sx[q];
+      z.ldw = int(r4(x.ns));
+      z.ldx = int(r4(std::max(x.nb, 1)));
+      z.w = off; off += int64_t(x.ns) * z.ldw;
+      z.wt = off; off += int64_t(x.ns) * z.ldw;
+      z.xt = off; off += int64_t(x.ns) * z.ldx;
+      // halving tree over the 64-blocks; levels[L] = nodes (a, m, b) at recursion depth L
+      const int nblk = nblocks(x.ns);
+      std::vector<std::array<int, 4>> stack{{0, nblk, 0, 0}};
+      while (!stack.empty()) {
+        auto nd = stack.back();
+        stack.pop_back();
+        const int a = nd[0], e = nd[1], L = nd[2];
+        if (e - a < 2) continue;
+        const int m = a + (e - a) / 2;
+        if (int(z.levels.size()) <= L) z.levels.resize(L + 1);
+        z.levels[L].push_back({a, m, e});
+        stack.push_back({a, m, L + 1, 0});
+        stack.push_back({m, e, L + 1, 0});
+      }
+      maxlev = std::max(maxlev, int(z.levels.size()));
+      int64_t tt_need = 0;
+      for (auto& lv : z.levels) {
+        int64_t sum = 0;
+        for (auto& nd : lv) {
+          const int64_t r0 = int64_t(nd[0]) * kNbk, r1 = int64_t(nd[1]) * kNbk;
+          const int64_t c0 = r1, c1 = std::min<int64_t>(int64_t(nd[2]) * kNbk, x.ns);
+          sum += (r1 - r0) * r4(c1 - c0);
+        }
+        tt_need = std::max(tt_need, sum);
+      }
+      z.tt = off; off += tt_need;
+      off = (off + 31) / 32 * 32;
+    }
+    scratch = std::max(scratch, off);
     {
       Op& o = b.begin(OP_ZGATHER);
       o.depth = d;
@@ -358,126 +444,133 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       }
       b.end();
     }
-    int steps = 0;
-    for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
-    // X = L_BS L_SS^-1, blocked right-looking from the last block column
-    for (int kb = steps - 1; kb >= 0; --kb) {
-      Op& o1 = b.begin(OP_GEMM);
-      o1.site = S_Z_XSOLVE; o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
-      o1.abuf = B_L; o1.bbuf = B_DINV; o1.cbuf = B_L;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.ns <= kb * kNbk || x.nb == 0) continue;
-        int w = std::min(kNbk, x.ns - kb * kNbk);
-        int64_t a = x.p_off + int64_t(x.ns) * x.ld + kb * kNbk;
-        b.gemm_tiles(a, x.ld, x.ld, x.d_off + int64_t(kb) * kNbk * kNbk, kNbk, 1, a, x.ld, x.nb, w, w);
+    {  // W, W^T start as zero, then take the inverse diagonal blocks
+      Op& o = b.begin(OP_MEMSET);
+      o.cbuf = B_SX;
+      o.elems = off;
+      b.end();
+      Op& oc = b.begin(OP_MIRROR);
+      oc.abuf = B_DINV; oc.cbuf = B_SX;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
+        for (int kb = 0; kb < nblocks(x.ns); ++kb) {
+          const int w = std::min(kNbk, x.ns - kb * kNbk);
+          const int64_t src = x.d_off + int64_t(kb) * kNbk * kNbk;
+          const int64_t dw = sx[q].w + int64_t(kb) * kNbk * sx[q].ldw + kb * kNbk;
+          const int64_t dwt = sx[q].wt + int64_t(kb) * kNbk * sx[q].ldw + kb * kNbk;
+          b.copy_tiles(src, kNbk, dw, sx[q].ldw, w, w, false);
+          b.copy_tiles(src, kNbk, dwt, sx[q].ldw, w, w, true);
+        }
       }
       b.end();
-      if (kb == 0) continue;
+    }
+    for (int L = maxlev - 1; L >= 0; --L) {
+      std::vector<int64_t> ttoff(fr.size(), 0);
+      Op& o1 = b.begin(OP_GEMM);  // TT = W_11^T L_21^T
+      o1.site = S_Z_XSOLVE; o1.mode = kStore; o1.al = kRow; o1.bl = kRow;
+      o1.abuf = B_SX; o1.bbuf = B_L; o1.cbuf = B_SX;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
+        if (int(sx[q].levels.size()) <= L) continue;
+        int64_t to = sx[q].tt;
+        for (auto& nd : sx[q].levels[L]) {
+          const int r0 = nd[0] * kNbk, r1 = nd[1] * kNbk, c1 = std::min(nd[2] * kNbk, x.ns);
+          const int ldt = int(r4(c1 - r1));
+          b.gemm_tiles(sx[q].wt + int64_t(r0) * sx[q].ldw + r0, sx[q].ldw, sx[q].ldw,
+                       x.p_off + int64_t(r1) * x.ld + r0, x.ld, x.ld, to, ldt, r1 - r0, c1 - r1, r1 - r0, false, 0,
+                       KT_A_UPPER);
+          to += int64_t(r1 - r0) * ldt;
+        }
+      }
+      b.end();
+      Op& o2 = b.begin(OP_GEMM);  // (W^T)_12 = -TT W_22^T
+      o2.site = S_Z_XUPD; o2.mode = kNegStore; o2.al = kRow; o2.bl = kRow;
+      o2.abuf = B_SX; o2.bbuf = B_SX; o2.cbuf = B_SX;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
+        if (int(sx[q].levels.size()) <= L) continue;
+        int64_t to = sx[q].tt;
+        for (auto& nd : sx[q].levels[L]) {
+          const int r0 = nd[0] * kNbk, r1 = nd[1] * kNbk, c1 = std::min(nd[2] * kNbk, x.ns);
+          const int ldt = int(r4(c1 - r1));
+          b.gemm_tiles(to, ldt, ldt, sx[q].w + int64_t(r1) * sx[q].ldw + r1, sx[q].ldw, sx[q].ldw,
+                       sx[q].wt + int64_t(r0) * sx[q].ldw + r1, sx[q].ldw, r1 - r0, c1 - r1, c1 - r1, false, 0,
+                       KT_B_LOWER);
+          to += int64_t(r1 - r0) * ldt;
+        }
+      }
+      b.end();
+      Op& om = b.begin(OP_MIRROR);  // W_21 = ((W^T)_12)^T
+      om.abuf = B_SX; om.cbuf = B_SX;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
+        if (int(sx[q].levels.size()) <= L) continue;
+        for (auto& nd : sx[q].levels[L]) {
+          const int r0 = nd[0] * kNbk, r1 = nd[1] * kNbk, c1 = std::min(nd[2] * kNbk, x.ns);
+          b.copy_tiles(sx[q].wt + int64_t(r0) * sx[q].ldw + r1, sx[q].ldw, sx[q].w + int64_t(r1) * sx[q].ldw + r0,
+                       sx[q].ldw, r1 - r0, c1 - r1, true);
+        }
+      }
+      b.end();
+    }
+    {  // X^T = W^T L_BS^T
+      Op& o = b.begin(OP_GEMM);
+      o.site = S_Z_XJ; o.mode = kStore; o.al = kRow; o.bl = kRow;
+      o.abuf = B_SX; o.bbuf = B_L; o.cbuf = B_SX;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
+        if (x.nb == 0) continue;
+        b.gemm_tiles(sx[q].wt, sx[q].ldw, sx[q].ldw, x.p_off + int64_t(x.ns) * x.ld, x.ld, x.ld, sx[q].xt, sx[q].ldx,
+                     x.ns, x.nb, x.ns, false, 0, KT_A_UPPER);
+      }
+      b.end();
+    }
+    {  // Z_SB = -X^T Z_BB
+      Op& o = b.begin(OP_GEMM);
+      o.site = S_Z_BS; o.mode = kNegStore; o.al = kRow; o.bl = kRow;
+      o.abuf = B_SX; o.bbuf = pz; o.cbuf = pz;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
+        if (x.nb == 0) continue;
+        b.gemm_tiles(sx[q].xt, sx[q].ldx, sx[q].ldx, x.z_off + int64_t(x.ns) * x.ldz + x.ns, x.ldz, x.ldz,
+                     x.z_off + x.ns, x.ldz, x.ns, x.nb, x.nb);
+      }
+      b.end();
+    }
+    {  // Z_SS = W^T W (lower tiles), then -= X^T Z_SB^T
+      Op& o = b.begin(OP_GEMM);
+      o.site = S_Z_JJ; o.mode = kStore; o.al = kRow; o.bl = kRow;
+      o.abuf = B_SX; o.bbuf = B_SX; o.cbuf = pz;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
+        b.gemm_tiles(sx[q].wt, sx[q].ldw, sx[q].ldw, sx[q].wt, sx[q].ldw, sx[q].ldw, x.z_off, x.ldz, x.ns, x.ns, x.ns,
+                     true, 0, KT_BOTH_UPPER);
+      }
+      b.end();
       Op& o2 = b.begin(OP_GEMM);
-      o2.site = S_Z_XUPD; o2.mode = kSub; o2.al = kRow; o2.bl = kCol;
-      o2.abuf = B_L; o2.bbuf = B_L; o2.cbuf = B_L;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.ns <= kb * kNbk || x.nb == 0) continue;
-        int w = std::min(kNbk, x.ns - kb * kNbk);
-        b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld + kb * kNbk, x.ld, x.ld, x.p_off + int64_t(kb) * kNbk * x.ld, x.ld,
-                     1, x.p_off + int64_t(x.ns) * x.ld, x.ld, x.nb, kb * kNbk, w);
-      }
-      b.end();
-    }
-    // Z_BS = -Z_BB X
-    {
-      Op& o = b.begin(OP_GEMM);
-      o.site = S_Z_BS; o.mode = kNegStore; o.al = kRow; o.bl = kCol;
-      o.abuf = pz; o.bbuf = B_L; o.cbuf = pz;
-      for (int f : fr) {
-        const Front& x = F[f];
+      o2.site = S_Z_SS; o2.mode = kSub; o2.al = kRow; o2.bl = kRow;
+      o2.abuf = B_SX; o2.bbuf = pz; o2.cbuf = pz;
+      for (size_t q = 0; q < fr.size(); ++q) {
+        const Front& x = F[fr[q]];
         if (x.nb == 0) continue;
-        b.gemm_tiles(x.z_off + int64_t(x.ns) * x.ldz + x.ns, x.ldz, x.ldz, x.p_off + int64_t(x.ns) * x.ld, x.ld, 1,
-                     x.z_off + int64_t(x.ns) * x.ldz, x.ldz, x.nb, x.ns, x.nb);
+        b.gemm_tiles(sx[q].xt, sx[q].ldx, sx[q].ldx, x.z_off + x.ns, x.ldz, x.ldz, x.z_off, x.ldz, x.ns, x.ns, x.nb,
+                     true);
       }
       b.end();
     }
-    // (L_SS L_SS^T)^-1 by the block-column Takahashi recursion, last block first
-    for (int J = steps - 1; J >= 0; --J) {
-      Op& ox = b.begin(OP_GEMM);  // X_J = L[R, J] Linv_J (in place)
-      ox.site = S_Z_XJ; ox.mode = kStore; ox.al = kRow; ox.bl = kCol;
-      ox.abuf = B_L; ox.bbuf = B_DINV; ox.cbuf = B_L;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.ns <= J * kNbk) continue;
-        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
-        if (nr <= 0) continue;
-        int64_t a = x.p_off + int64_t(R0) * x.ld + J * kNbk;
-        b.gemm_tiles(a, x.ld, x.ld, x.d_off + int64_t(J) * kNbk * kNbk, kNbk, 1, a, x.ld, nr, w, w);
-      }
-      b.end();
-      Op& oz = b.begin(OP_GEMM);  // Z[R, J] = -Z[R, R] X_J
-      oz.site = S_Z_RJ; oz.mode = kNegStore; oz.al = kRow; oz.bl = kCol;
-      oz.abuf = pz; oz.bbuf = B_L; oz.cbuf = pz;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.ns <= J * kNbk) continue;
-        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
-        if (nr <= 0) continue;
-        b.gemm_tiles(x.z_off + int64_t(R0) * x.ldz + R0, x.ldz, x.ldz, x.p_off + int64_t(R0) * x.ld + J * kNbk, x.ld, 1,
-                     x.z_off + int64_t(R0) * x.ldz + J * kNbk, x.ldz, nr, w, nr);
-      }
-      b.end();
-      Op& oj = b.begin(OP_GEMM);  // Z[J, J] = Linv_J^T Linv_J
-      oj.site = S_Z_JJ; oj.mode = kStore; oj.al = kCol; oj.bl = kCol;
-      oj.abuf = B_DINV; oj.bbuf = B_DINV; oj.cbuf = pz;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.ns <= J * kNbk) continue;
-        int w = std::min(kNbk, x.ns - J * kNbk);
-        int64_t dj = x.d_off + int64_t(J) * kNbk * kNbk;
-        b.gemm_tiles(dj, kNbk, 1, dj, kNbk, 1, x.z_off + int64_t(J) * kNbk * x.ldz + J * kNbk, x.ldz, w, w, w);
-      }
-      b.end();
-      Op& oj2 = b.begin(OP_GEMM);  // Z[J, J] -= X_J^T Z[R, J]
-      oj2.site = S_Z_JJ2; oj2.mode = kSub; oj2.al = kCol; oj2.bl = kCol;
-      oj2.abuf = B_L; oj2.bbuf = pz; oj2.cbuf = pz;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.ns <= J * kNbk) continue;
-        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
-        if (nr <= 0) continue;
-        b.gemm_tiles(x.p_off + int64_t(R0) * x.ld + J * kNbk, x.ld, 1, x.z_off + int64_t(R0) * x.ldz + J * kNbk,
-                     x.ldz, 1, x.z_off + int64_t(J) * kNbk * x.ldz + J * kNbk, x.ldz, w, w, nr);
-      }
-      b.end();
-      Op& om = b.begin(OP_MIRROR);  // Z[J, R] = Z[R, J]^T
-      om.cbuf = pz;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.ns <= J * kNbk) continue;
-        int w = std::min(kNbk, x.ns - J * kNbk), R0 = J * kNbk + w, nr = x.ns - R0;
-        if (nr <= 0) continue;
-        b.mirror_tiles(x.z_off + int64_t(R0) * x.ldz + J * kNbk, x.z_off + int64_t(J) * kNbk * x.ldz + R0, x.ldz, nr,
-                       w);
-      }
-      b.end();
-    }
-    // Z_SS -= X^T Z_BS, then Z_SB = Z_BS^T
-    {
-      Op& o = b.begin(OP_GEMM);
-      o.site = S_Z_SS; o.mode = kSub; o.al = kCol; o.bl = kCol;
-      o.abuf = B_L; o.bbuf = pz; o.cbuf = pz;
-      for (int f : fr) {
-        const Front& x = F[f];
-        if (x.nb == 0) continue;
-        b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld, x.ld, 1, x.z_off + int64_t(x.ns) * x.ldz, x.ldz, 1, x.z_off, x.ldz,
-                     x.ns, x.ns, x.nb);
-      }
-      b.end();
+    {  // upper triangle of Z_SS from the strictly lower tiles; Z_BS = Z_SB^T
       Op& om = b.begin(OP_MIRROR);
-      om.cbuf = pz;
+      om.abuf = pz; om.cbuf = pz;
       for (int f : fr) {
         const Front& x = F[f];
-        if (x.nb == 0) continue;
-        b.mirror_tiles(x.z_off + int64_t(x.ns) * x.ldz, x.z_off + x.ns, x.ldz, x.nb, x.ns);
+        for (int j0 = 0; j0 < x.ns; j0 += TN)
+          for (int i0 = j0 + TM; i0 < x.ns; i0 += TM) {
+            const int rows = std::min(TM, x.ns - i0), cols = std::min(TN, x.ns - j0);
+            b.copy_tiles(x.z_off + int64_t(i0) * x.ldz + j0, x.ldz, x.z_off + int64_t(j0) * x.ldz + i0, x.ldz, rows,
+                         cols, true);
+          }
+        if (x.nb > 0)
+          b.copy_tiles(x.z_off + x.ns, x.ldz, x.z_off + int64_t(x.ns) * x.ldz, x.ldz, x.ns, x.nb, true);
       }
       b.end();
     }
@@ -490,6 +583,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       b.end();
     }
   }
+  *scratch_elems = scratch;
 }
 
 // ------------------------------------------------------------ small kernels
@@ -549,15 +643,20 @@ __global__ void zgather_kernel(const RowTask* __restrict__ tasks, const DevFront
 }
 
 template <typename T>
-__global__ void mirror_kernel(const MirrorTask* __restrict__ tasks, T* __restrict__ Z) {
+__global__ void mirror_kernel(const MirrorTask* __restrict__ tasks, const T* src, T* dst) {
   __shared__ T tile[32][33];
   const MirrorTask tk = tasks[blockIdx.x];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   for (int i = ty; i < 32; i += 8)
-    if (i < tk.rows && tx < tk.cols) tile[i][tx] = Z[tk.src + int64_t(i) * tk.ld + tx];
+    if (i < tk.rows && tx < tk.cols) tile[i][tx] = src[tk.src + int64_t(i) * tk.lds + tx];
   __syncthreads();
-  for (int j = ty; j < 32; j += 8)
-    if (j < tk.cols && tx < tk.rows) Z[tk.dst + int64_t(j) * tk.ld + tx] = tile[tx][j];
+  if (tk.trans) {
+    for (int j = ty; j < 32; j += 8)
+      if (j < tk.cols && tx < tk.rows) dst[tk.dst + int64_t(j) * tk.ldd + tx] = tile[tx][j];
+  } else {
+    for (int i = ty; i < 32; i += 8)
+      if (i < tk.rows && tx < tk.cols) dst[tk.dst + int64_t(i) * tk.ldd + tx] = tile[i][tx];
+  }
 }
 
 template <typename T>
@@ -690,6 +789,7 @@ struct Exec {
       case B_W1: return static_cast<T*>(p->d_W[1]);
       case B_G0: return static_cast<T*>(p->d_G[0]);
       case B_G1: return static_cast<T*>(p->d_G[1]);
+      case B_SX: return static_cast<T*>(p->d_sx);
       default: return nullptr;
     }
   }
@@ -729,7 +829,9 @@ struct Exec {
                                                      buf(pd ? B_P1 : B_P0));
           break;
         }
-        case OP_MIRROR: mirror_kernel<T><<<o.count, 256, 0, st>>>(s.d_mirror + o.off, buf(o.cbuf)); break;
+        case OP_MIRROR:
+          mirror_kernel<T><<<o.count, 256, 0, st>>>(s.d_mirror + o.off, buf(o.abuf), buf(o.cbuf));
+          break;
         case OP_ZEXTRACT:
           zextract_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, p->d_iperm, p->d_amap,
                                                       p->sym.nslots, buf(o.cbuf), zq);
@@ -775,7 +877,9 @@ int plan_build(Plan* p) {
     CUDA_TRY(cudaMalloc(&p->d_pool[k], size_t(p->pool_elems[k]) * es));
   }
   build_factor_schedule(S, p->sched_factor, TM, TM);
-  build_selinv_schedule(S, p->sched_selinv, TM, TM);
+  int64_t sx_elems = 0;
+  build_selinv_schedule(S, p->sched_selinv, TM, TM, &sx_elems);
+  CUDA_TRY(cudaMalloc(&p->d_sx, size_t(sx_elems) * es));
   p->sched_factor.upload();
   p->sched_selinv.upload();
   CUDA_TRY(cudaMalloc(&p->d_logpiv, std::max<size_t>(p->sched_factor.diag.size(), 1) * sizeof(double)));

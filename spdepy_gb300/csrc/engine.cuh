@@ -16,7 +16,7 @@ namespace spde {
 enum OpKind {
   OP_MEMSET = 0, OP_EXTEND, OP_DIAG, OP_GEMM, OP_SGATHER_FWD, OP_SGATHER_BWD, OP_ZGATHER, OP_MIRROR, OP_ZEXTRACT
 };
-enum BufId { B_NONE = 0, B_L, B_DINV, B_P0, B_P1, B_X, B_W0, B_W1, B_G0, B_G1 };
+enum BufId { B_NONE = 0, B_L, B_DINV, B_P0, B_P1, B_X, B_W0, B_W1, B_G0, B_G1, B_SX };
 
 // Call sites of the tiled product (for per-site timing).
 enum GemmSite {
@@ -37,10 +37,11 @@ struct Op {
   int depth = 0;
 };
 
-// Rectangle transpose: dst[j*ld + i] = src[i*ld + j], i < rows, j < cols (one 32x32 tile per task).
+// 32 x 32 block copy, rows x cols of src: dst[j*ldd + i] = src[i*lds + j] when
+// trans, else dst[i*ldd + j] = src[i*lds + j].
 struct MirrorTask {
   int64_t src, dst;
-  int ld, rows, cols;
+  int lds, ldd, rows, cols, trans;
 };
 // Front-wide task over a row range (gathers, extraction).
 struct RowTask {
@@ -78,6 +79,7 @@ struct Plan {
   void* d_L = nullptr;
   void* d_dinv = nullptr;
   void* d_pool[2] = {nullptr, nullptr};
+  void* d_sx = nullptr;  // selected-inversion scratch (triangular inverse, X^T)
   int64_t pool_elems[2] = {0, 0};
   double* d_logpiv = nullptr;
   int* d_err = nullptr;
