@@ -141,6 +141,18 @@ int spde_selinv(SpdePlan* plan, double* zq_dev);
 /* d/dtheta <Gbar, Q(theta)> for a symmetric Gbar in stencil layout (device
  * FP64); grad_host receives ntheta-1 values (all but log tau). */
 int spde_adjoint(SpdePlan* plan, const double* gbar_dev, double* grad_host);
+/* The same gradient without any device allocation (no reference counterpart).
+ * For callers that cannot call cudaMalloc during the computation, e.g. code
+ * that runs under a framework owning all device memory through its own pool,
+ * or code that must not synchronise the device mid-stream (cudaMalloc and
+ * cudaFree can).  The caller passes Gbar and receives ntheta-1 values in
+ * grad_dev (both device FP64); the work array is a fixed 8 MiB static device
+ * array, enough for grids with Mx*Ny <= 9892 cells (larger grids return
+ * SPDE_ERR_ARG).  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (other streams, other host threads, other plans) race on it. */
+int spde_adjoint_noalloc(SpdePlan* plan, const double* gbar_dev, double* grad_dev);
 
 /* ---- log-likelihood and gradient: logLike (spdes/advection_diffusion2D.py:187-223).
  * y_dev: m x r observations (device FP64, row-major, in spde_set_obs order).

@@ -70,6 +70,7 @@ SIGNATURES = {
     "spde_sample": (_I, [_P, _P, _P, _I]),
     "spde_selinv": (_I, [_P, _P]),
     "spde_adjoint": (_I, [_P, _P, _P]),
+    "spde_adjoint_noalloc": (_I, [_P, _P, _P]),
     "spde_loglike": (_I, [_P, _P, _I, _P, _I, _I, _P, _I, ctypes.POINTER(_D), _P]),
     "spde_conditional_mean": (_I, [_P, _D, _P, _P, _P]),
 }

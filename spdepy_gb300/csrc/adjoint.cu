@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <mutex>
+
 #include "engine.cuh"
 #include "stencil.cuh"
 
@@ -341,6 +343,31 @@ __global__ void coef_reduce_kernel(DevModel m, const double* __restrict__ cg, do
 }
 
 int64_t adjoint_work_elems(const Plan* p) { return int64_t(p->sym.Mx) * p->sym.Ny * (84 + kCW); }
+
+// ---------------------------------------------------------------------------
+// Fixed scratch of the allocation-free adjoint entry point (spde_adjoint_noalloc).
+// It lives in the module's static device memory: every GPU that loads this
+// library holds these 8 MiB until the process exits.  In host code the symbol is
+// only a stand-in, so its device address is looked up once per device, with that
+// device current, and cached.
+constexpr int64_t kNoAllocElems = int64_t(1) << 20;  // doubles
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocElems];
+
+int noalloc_scratch(double** ptr, int64_t* elems) {
+  static std::mutex mu;
+  static double* cache[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!cache[dev]) {
+    void* addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_noalloc_scratch) != cudaSuccess || !addr) return 1;
+    cache[dev] = static_cast<double*>(addr);
+  }
+  *ptr = cache[dev];
+  *elems = kNoAllocElems;
+  return 0;
+}
 
 void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st) {
   const int Ns = p->sym.Mx * p->sym.Ny;

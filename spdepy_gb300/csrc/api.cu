@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <string>
 #include <new>
 #include <vector>
 
@@ -451,6 +452,27 @@ int spde_adjoint(SpdePlan* plan, const double* gbar, double* grad_host) {
   cudaFree(work);
   cudaFree(g);
   if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) { p.last_error = "adjoint failed"; return SPDE_ERR_CUDA; }
+  return SPDE_OK;
+}
+
+int spde_adjoint_noalloc(SpdePlan* plan, const double* gbar, double* grad_dev) {
+  if (!plan || !gbar || !grad_dev) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  double* scratch = nullptr;
+  int64_t cap = 0;
+  if (noalloc_scratch(&scratch, &cap)) { p.last_error = "fixed scratch not reachable on this device"; return SPDE_ERR_CUDA; }
+  const int64_t need = adjoint_work_elems(&p);
+  if (need > cap) {
+    p.last_error = "grid too large for the fixed adjoint scratch (needs " + std::to_string(need) +
+                   " doubles, limit " + std::to_string(cap) + ", i.e. Mx*Ny <= " + std::to_string(cap / 106) + ")";
+    return SPDE_ERR_ARG;
+  }
+  // the kernels write every scratch entry they later read; clear anyway so no
+  // value from an earlier call can leak into this one
+  API_CUDA(cudaMemsetAsync(scratch, 0, size_t(need) * sizeof(double), p.stream));
+  launch_adjoint(&p, gbar, grad_dev, scratch, p.stream);
+  API_CUDA(cudaGetLastError());
   return SPDE_OK;
 }
 

@@ -148,5 +148,6 @@ void prof_collect(Plan* p);
 // adjoint (adjoint.cu)
 void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st);
 int64_t adjoint_work_elems(const Plan* p);
+int noalloc_scratch(double** ptr, int64_t* elems);
 
 }  // namespace spde
