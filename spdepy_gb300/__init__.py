@@ -10,7 +10,13 @@ from .grids import Grid, grid
 from .model import Model
 from .spdes import spde_init
 
-__all__ = ["grid", "Grid", "model", "Model", "spde_init"]
+__all__ = ["grid", "Grid", "model", "Model", "spde_init", "loglike"]
+
+
+def loglike(model, par, grad_mode="exact"):
+    """Differentiable log-likelihood objective (torch.autograd.Function)."""
+    from .autograd import loglike as _ll
+    return _ll(model, par, grad_mode)
 
 
 def model(**kwargs) -> Model:

@@ -12,7 +12,9 @@
 #include <algorithm>
 #include <array>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "engine.cuh"
 
@@ -771,6 +773,29 @@ void prof_collect(Plan* p) {
   p->ev_used = 0;
 }
 
+// Optional launch log of the tensor-core tiled product: with SPDE_LAUNCH_LOG set
+// to a file name, one line per launch (process-wide launch number, call site,
+// tiles, algorithmic flops), so that a profiler capture of the n-th launch can be
+// matched with the work it did.  Host-side bookkeeping only.
+static void tc_launch_log(const Op& o) {
+  static std::mutex mu;
+  static FILE* fh = nullptr;
+  static bool opened = false;
+  static int64_t seq = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!opened) {
+    opened = true;
+    const char* path = std::getenv("SPDE_LAUNCH_LOG");
+    if (path && *path) fh = std::fopen(path, "w");
+    if (fh) std::fprintf(fh, "launch site tiles flops\n");
+  }
+  if (fh) {
+    std::fprintf(fh, "%lld %d %d %.0f\n", static_cast<long long>(seq), o.site, o.count, o.flops);
+    std::fflush(fh);
+  }
+  ++seq;
+}
+
 // ------------------------------------------------------------------ executor
 template <typename T>
 struct Exec {
@@ -810,6 +835,7 @@ struct Exec {
         case OP_GEMM:
           launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st,
                          o.tc != 0);
+          if (sizeof(T) == sizeof(float) && o.tc && tc_gemm_enabled()) tc_launch_log(o);
           break;
         case OP_SGATHER_FWD: {
           int pd = o.depth & 1;

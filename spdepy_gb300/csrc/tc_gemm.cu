@@ -1,16 +1,25 @@
 // Tiled product on the 5th-generation tensor cores (tcgen05) for FP32 fronts.
 //
 // One CTA computes one 128 x 128 output tile of C (op)= A B' (the GemmTask
-// contract of dense.cu).  The accumulator lives in tensor memory (128 TMEM
-// columns, FP32).  K advances in chunks of 32 FP32 values staged by cp.async
-// straight into 128-byte-swizzled K-major shared-memory tiles, two chunks ahead
-// of the tensor core (four raw stages).  The tensor core reads a raw FP32 tile as
-// TF32 (it drops the 13 low mantissa bits: hi = trunc(x)); the threads write the
-// exact residual x - hi, rounded to TF32, into a second plane, and one elected
-// thread issues, per 8-wide k step, hi*hi + hi*lo + lo*hi (the lo*lo term,
-// ~2^-21 relative, is dropped), which gives FP32-class products.
-// Warps 0-3 stage, convert and write back; warp 4 issues the MMAs; they hand
-// stages over through mbarriers (tcgen05.commit arrives when MMAs finish).
+// contract of dense.cu).  The accumulator lives in tensor memory (TMEM columns
+// 0-127, FP32).  K advances in chunks of 32 FP32 values staged by cp.async into
+// 128-byte-swizzled K-major shared-memory tiles, three chunks ahead of the tensor
+// core (four stages).  Each product runs as 3xTF32: the tensor core reads
+// operands as TF32, so every operand is split into hi = trunc(x) (the 19 high
+// bits) and lo = x - hi rounded to TF32, and one elected thread issues, per
+// 8-wide k step, hi*hi + hi*lo + lo*hi (the lo*lo term, ~2^-21 relative, is
+// dropped), which gives FP32-class products.
+//
+// Operand A goes to the tensor core from TMEM: two threads of the eight
+// converter warps own row r of the tile (TMEM lane r), read its 32 raw values of
+// the chunk from shared memory and store hi and lo with tcgen05.st into one of
+// two 64-column TMEM slots (columns 128-255).  Only operand B (raw plane as hi, plus
+// a residual plane) is read by the tensor core from shared memory, which takes
+// the A reads, the A residual writes and half of the tensor core's operand
+// reads off the shared-memory port.
+// Warps 0-7 stage, convert and run the epilogue (two warps per SM sub-partition
+// hide the latency of the conversion); warp 8 issues the MMAs; they hand chunks
+// over through mbarriers (tcgen05.commit arrives when MMAs finish).
 // Every wait is bounded by a wall-clock limit, after which the CTA records an
 // error, frees its tensor memory and returns.
 #include <cuda_runtime.h>
@@ -23,12 +32,15 @@ namespace spde {
 namespace {
 
 constexpr int kTM = 128, kTN = 128, kTK = 32;
-constexpr int kConv = 128;                 // loader / converter / epilogue threads (warps 0-3)
+constexpr int kConv = 256;                 // loader / converter / epilogue threads (warps 0-7)
 constexpr int kThreads = kConv + 32;       // + one MMA warp
 constexpr int kPlane = 128 * 32 * 4;       // one 128 x 32 FP32 operand plane (16 KB)
-constexpr int kStages = 3;                 // stage = raw A, raw B, residual A, residual B
-constexpr int kStageBytes = 4 * kPlane;
+constexpr int kStages = 4;                 // stage = raw A, raw B, residual B
+constexpr int kAhead = 3;                  // chunks staged ahead of the converters
+constexpr int kStageBytes = 3 * kPlane;
 constexpr int kSmem = kStages * kStageBytes + 1024;
+constexpr int kTmemCols = 256;             // accumulator 0-127, A slots 128-191 and 192-255
+constexpr int kASlot0 = 128, kASlotCols = 64;
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
 
 __device__ int g_tc_error = 0;
@@ -71,11 +83,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t(kTN) >> 3) << 17) |
                             ((uint32_t(kTM) >> 4) << 24);
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t acc) {
+// D (TMEM) (+)= A (TMEM, lane = row, one column per k) * B (shared memory descriptor)
+__device__ __forceinline__ void mma_tf32_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t b, uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "r"(tmem_a), "l"(b), "r"(kIdesc), "r"(acc));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -172,21 +185,40 @@ __device__ __forceinline__ void stage_raw(const float* X, int64_t ld, int rows, 
   }
 }
 
-// Residual planes of one stage.  With cp.async staging every thread converts
-// exactly the chunks it copied (its own completed copies are all it needs);
-// register-staged layouts are followed by a loader-wide barrier first.
-__device__ __forceinline__ void split_stage(const uint8_t* raw, uint8_t* lo, int tid) {
+// Residual plane of operand B for one stage: loader thread `tid` converts the
+// 16-byte chunks q = tid + i * kConv.
+__device__ __forceinline__ void split_b(const uint8_t* raw, uint8_t* lo, int tid) {
 #pragma unroll
-  for (int plane = 0; plane < 2; ++plane)
+  for (int it = 0; it < 1024 / kConv; ++it) {
+    const int q = tid + it * kConv;
+    const uint32_t off = sw_chunk(q >> 3, q & 7);
+    const float4 v = *reinterpret_cast<const float4*>(raw + off);
+    *reinterpret_cast<float4*>(lo + off) =
+        make_float4(tf32_resid(v.x), tf32_resid(v.y), tf32_resid(v.z), tf32_resid(v.w));
+  }
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]) : "memory");
+}
+
+// Half `h` (k = 16 h .. 16 h + 15) of row `row` of the raw A plane into TMEM lane
+// `row`: hi = trunc(x) in columns col + 16 h .., lo = rna(x - hi) in col + 32 + 16 h ..
+__device__ __forceinline__ void a_to_tmem(const uint8_t* raw, int row, int h, uint32_t taddr) {
+  uint32_t hi[16], lo[16];
 #pragma unroll
-    for (int it = 0; it < 1024 / kConv; ++it) {
-      const int q = tid + it * kConv;
-      const int r = q >> 3, c4 = q & 7;
-      const uint32_t off = uint32_t(plane * kPlane) + sw_chunk(r, c4);
-      float4 v = *reinterpret_cast<const float4*>(raw + off);
-      *reinterpret_cast<float4*>(lo + off) =
-          make_float4(tf32_resid(v.x), tf32_resid(v.y), tf32_resid(v.z), tf32_resid(v.w));
+  for (int c = 0; c < 4; ++c) {
+    const float4 v = *reinterpret_cast<const float4*>(raw + sw_chunk(row, 4 * h + c));
+    const float x[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const uint32_t hb = __float_as_uint(x[e]) & 0xFFFFE000u;
+      hi[4 * c + e] = hb;
+      lo[4 * c + e] = __float_as_uint(tf32_rna(x[e] - __uint_as_float(hb)));
     }
+  }
+  tmem_st16(taddr + 16 * h, hi);
+  tmem_st16(taddr + 32 + 16 * h, lo);
 }
 
 __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
@@ -209,14 +241,15 @@ __device__ __forceinline__ bool loader_all(bool v) {
 template <int MODE, int AL, int BL>
 __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __restrict__ tasks, const float* Ab,
                                                               const float* Bb, float* Cb) {
-  // Warps 0-3 stage chunks (cp.async), write the residual planes and run the
-  // epilogue; warp 4 issues the MMAs.  Per stage s: `ready[s]` (kConv arrivals)
-  // says the stage is converted, `free_[s]` (tcgen05.commit) says its MMAs are
-  // done; `done` follows the last MMA.
+  // Warps 0-7 stage chunks (cp.async), convert them (A to TMEM, B residual to
+  // shared memory) and run the epilogue; warp 8 issues the MMAs.  Per stage s:
+  // `ready[s]` (kConv arrivals) says chunk t (t % kStages == s) is converted,
+  // `consumed[s]` (tcgen05.commit) says its MMAs are done; `done` follows the
+  // last MMA.
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t ready[kStages], free_[kStages], done;
+  __shared__ uint64_t ready[kStages], consumed[kStages], done;
   __shared__ uint32_t tmem_slot;
-  __shared__ int abort_flag;
+  __shared__ int abort_flag, mma_issued;
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const GemmTask tk = tasks[blockIdx.x];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -225,19 +258,20 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
   float* C = Cb + tk.c;
   const bool avec = ((reinterpret_cast<uintptr_t>(A) & 15) == 0) && ((tk.lda & 3) == 0);
   const bool bvec = ((reinterpret_cast<uintptr_t>(B) & 15) == 0) && ((tk.ldb & 3) == 0);
-  const bool async_a = AL == kRow && avec, async_b = BL == kRow && bvec;
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&ready[s])), "r"(kConv));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&free_[s])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&consumed[s])));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
+    mma_issued = 0;
   }
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&tmem_slot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     asm volatile("tcgen05.fence::before_thread_sync;");
   }
@@ -246,11 +280,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
   const uint32_t tmem = tmem_slot;
   const int nk = (tk.k + kTK - 1) / kTK;
 
-  auto wait = [&](uint64_t* bar, uint32_t parity) -> bool {
+  // bounded wait; with `honor_abort` it also gives up as soon as another thread
+  // of the CTA has recorded a failure
+  auto wait = [&](uint64_t* bar, uint32_t parity, bool honor_abort) -> bool {
     if (mbar_try(smem_u32(bar), parity)) return true;
     const unsigned long long t0 = now_ns();
     while (!mbar_try(smem_u32(bar), parity)) {
-      if (*(volatile int*)&abort_flag) return false;
+      if (honor_abort && *(volatile int*)&abort_flag) return false;
       if (now_ns() - t0 > kWaitNs) {
         atomicExch(&abort_flag, 1);
         return false;
@@ -259,46 +295,56 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
     return true;
   };
 
-  if (warp < 4) {
+  if (warp < kConv / 32) {
     // ---------------- loaders / converters
-    for (int t = 0; t < 2 && t < nk; ++t) {
-      uint8_t* st = smem + t * kStageBytes;
-      stage_raw<AL>(A, tk.lda, tk.m, t * kTK, tk.k, avec, st, tid);
-      stage_raw<BL>(B, tk.ldb, tk.n, t * kTK, tk.k, bvec, st + kPlane, tid);
+    for (int t = 0; t < kAhead; ++t) {
+      if (t < nk) {
+        uint8_t* st = smem + t * kStageBytes;
+        stage_raw<AL>(A, tk.lda, tk.m, t * kTK, tk.k, avec, st, tid);
+        stage_raw<BL>(B, tk.ldb, tk.n, t * kTK, tk.k, bvec, st + kPlane, tid);
+      }
       cp_async_commit();
     }
+    bool ok = true;
     for (int t = 0; t < nk; ++t) {
       const int s = t % kStages;
       uint8_t* st = smem + s * kStageBytes;
-      if (t + 1 < nk) cp_async_wait<1>(); else cp_async_wait<0>();
-      if (!(async_a && async_b) && !loader_all(true)) break;
-      split_stage(st, st + 2 * kPlane, tid);
+      cp_async_wait<kAhead - 1>();  // this thread's copies of chunk t have landed
+      // TMEM slot t & 1 was last read by chunk t - 2
+      if (t >= 2) ok = ok && wait(&consumed[(t - 2) % kStages], uint32_t(((t - 2) / kStages) & 1), true);
+      // all copies of the chunk visible to every converter; failures end the loop together
+      if (!loader_all(ok)) break;
+      // warp w reaches TMEM lanes 32 (w % 4) ..; warps 0-3 take k 0-15, warps 4-7 k 16-31
+      a_to_tmem(st, tid & 127, tid >> 7,
+                tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(kASlot0 + (t & 1) * kASlotCols));
+      split_b(st + kPlane, st + 2 * kPlane, tid);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(smem_u32(&ready[s]));
-      if (t + 2 < nk) {
-        const int s2 = (t + 2) % kStages;  // last used by chunk t - 1
-        const bool ok = t < 1 || wait(&free_[s2], uint32_t(((t - 1) / kStages) & 1));
-        if (async_a && async_b) {
-          if (!ok) break;
-        } else if (!loader_all(ok)) {
-          break;
+      const int tn = t + kAhead;
+      if (tn < nk) {
+        // stage tn % kStages last held chunk t - 1, whose MMAs read its B planes
+        if (t >= 1) ok = ok && wait(&consumed[(t - 1) % kStages], uint32_t(((t - 1) / kStages) & 1), true);
+        if (ok) {
+          uint8_t* st2 = smem + (tn % kStages) * kStageBytes;
+          stage_raw<AL>(A, tk.lda, tk.m, tn * kTK, tk.k, avec, st2, tid);
+          stage_raw<BL>(B, tk.ldb, tk.n, tn * kTK, tk.k, bvec, st2 + kPlane, tid);
         }
-        uint8_t* st2 = smem + s2 * kStageBytes;
-        stage_raw<AL>(A, tk.lda, tk.m, (t + 2) * kTK, tk.k, avec, st2, tid);
-        stage_raw<BL>(B, tk.ldb, tk.n, (t + 2) * kTK, tk.k, bvec, st2 + kPlane, tid);
       }
       cp_async_commit();
     }
     cp_async_wait<0>();
-    const bool ok = nk == 0 || wait(&done, 0u);
-    if (ok) {
+    const bool fin = nk == 0 || wait(&done, 0u, true);
+    if (fin) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const int row = warp * 32 + lane;
+      // warp w reads lanes 32 (w % 4) .. and accumulator columns 64 (w / 4) .. + 63
+      const int row = (warp & 3) * 32 + lane;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const int col0 = c * 32;
+      for (int c = 0; c < 2; ++c) {
+        const int col0 = (warp >> 2) * 64 + c * 32;
         uint32_t r[32];
-        const uint32_t ta = tmem + (uint32_t(warp * 32) << 16) + uint32_t(col0);
+        const uint32_t ta = tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(col0);
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -344,26 +390,32 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
     // ---------------- MMA issuer
     for (int t = 0; t < nk; ++t) {
       const int s = t % kStages;
-      if (!wait(&ready[s], uint32_t((t / kStages) & 1))) break;
+      if (!wait(&ready[s], uint32_t((t / kStages) & 1), true)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t ra = smem_u32(smem + s * kStageBytes), la = ra + 2 * kPlane;
+      const uint32_t rb = smem_u32(smem + s * kStageBytes + kPlane), lb = rb + kPlane;
+      const uint32_t ah = tmem + uint32_t(kASlot0 + (t & 1) * kASlotCols), al = ah + 32;
 #pragma unroll
       for (int kk = 0; kk < kTK / 8; ++kk) {
-        const uint64_t ah = smem_desc(ra + kk * 32), bh = smem_desc(ra + kPlane + kk * 32);
-        const uint64_t al = smem_desc(la + kk * 32), bl = smem_desc(la + kPlane + kk * 32);
-        mma_tf32(tmem, ah, bh, (t > 0 || kk > 0) ? 1u : 0u);
-        mma_tf32(tmem, ah, bl, 1u);
-        mma_tf32(tmem, al, bh, 1u);
+        const uint64_t bh = smem_desc(rb + kk * 32), bl = smem_desc(lb + kk * 32);
+        mma_tf32_ts(tmem, ah + kk * 8, bh, (t > 0 || kk > 0) ? 1u : 0u);
+        mma_tf32_ts(tmem, ah + kk * 8, bl, 1u);
+        mma_tf32_ts(tmem, al + kk * 8, bh, 1u);
       }
-      mma_commit(smem_u32(&free_[s]));
+      mma_commit(smem_u32(&consumed[s]));
+      mma_issued = 1;
     }
-    if (nk > 0) mma_commit(smem_u32(&done));
+    // `done` tracks every MMA issued, also after a failure, so the clean-up can
+    // wait for them before the tensor memory is freed
+    if (mma_issued) mma_commit(smem_u32(&done));
   }
   __syncthreads();
-  if (tid == 0 && abort_flag) atomicExch(&g_tc_error, 1);
+  if (tid == 0 && abort_flag) {
+    atomicExch(&g_tc_error, 1);
+    if (mma_issued) wait(&done, 0u, false);
+  }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemCols));
 }
 
 template <int MODE, int AL, int BL>

@@ -429,6 +429,7 @@ class SpdeModel:
         self.r = data.shape[1] if data.ndim == 2 else 1
         self.idx = kwargs.get("idx")
         self.S = self.grid.getS(self.idx)
+        self._y_pinned = None
         x0 = self.layout.defaults()
         if self.fitQ0 and self.mod0 is not None:
             x0 = np.hstack([x0[:-1], self.mod0.getPars()[:-1], x0[-1]])
@@ -442,8 +443,10 @@ class SpdeModel:
         if self.data is None:
             raise RuntimeError("call initFit(data, idx=...) first")
         self._ensure_model()
-        self.plan.set_obs(self.grid.obs_nodes(self.idx))
-        y = torch.as_tensor(self.data.reshape(-1, self.r))
+        self.plan.set_obs(self.grid.obs_nodes(self.idx))  # uploads only when the index changed
+        if getattr(self, "_y_pinned", None) is None:
+            self._y_pinned = torch.as_tensor(np.ascontiguousarray(self.data.reshape(-1, self.r))).pin_memory()
+        y = self._y_pinned.to("cuda", non_blocking=True)
         canon = self.canonical(par)
         mode = 0
         probes = None
