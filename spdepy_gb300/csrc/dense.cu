@@ -138,96 +138,189 @@ template void launch_gemm<float>(const GemmTask*, int, const float*, const float
                                  cudaStream_t, bool);
 
 // --------------------------------------------------- diagonal block POTRF
-// The block is factored in FP64 in shared memory whatever the storage type, so
-// the pivots (and the log-determinant) carry FP64 arithmetic.
+// Cholesky factor and inverse of one w x w diagonal block (w <= 64) per CTA.
+//
+// The factorisation runs in FP64 whatever the storage type, so the pivots and
+// the log-determinant carry FP64 arithmetic (an FP32 sweep measured 1e-6
+// relative log-likelihood error against 1e-7 at 960k nodes).  FP64 is a narrow
+// pipe on this part, so the sweep is arranged around it: the block lives in the
+// registers of 256 threads, thread (ty, tx) = (tid / 16, tid % 16) owning the
+// entries (i, k) = (ty + 16 m, tx + 16 n), m, n = 0..3.  Step j reads column j of
+// the partly reduced block from a shared buffer, applies
+// a_ik -= a_ij a_kj / a_jj (j < k <= i) and publishes column j + 1, one barrier
+// per column and one FP64 division per warp; square roots come at the end:
+// L_ij = a_ij / sqrt(d_j) and log L_jj = log(d_j) / 2 with d_j the j-th pivot.
+// L^-1 (consumed by the panel products as a product operand) then follows by
+// forward elimination in the storage type's arithmetic with the same ownership.
 constexpr int kMaxNbk = 64;
 
-
-// Arithmetic type A (FP64 on both paths; an FP32 sweep measured 1e-6 relative
-// log-likelihood error against 1e-7 for FP64 at 960k nodes).  The logs of the
-// pivots are taken in parallel after the sweep and summed in FP64.
-template <typename T, typename A>
+template <typename T>
 __global__ void __launch_bounds__(256) potrf_kernel(const DiagTask* __restrict__ tasks, T* __restrict__ L,
                                                     T* __restrict__ dinv, double* __restrict__ logpiv,
                                                     int* __restrict__ err) {
-  // Right-looking Cholesky of the block and, in the same sweep, forward
-  // elimination of [L | I] for L^-1: after the pivot of column j, row j of the
-  // inverse is R_j / L_jj and every later row i drops L_ij times it.
-  extern __shared__ __align__(16) unsigned char dsm_raw[];
-  A* dsm = reinterpret_cast<A*>(dsm_raw);
-  A(*a)[kMaxNbk + 1] = reinterpret_cast<A(*)[kMaxNbk + 1]>(dsm);
-  A(*x)[kMaxNbk + 1] = reinterpret_cast<A(*)[kMaxNbk + 1]>(dsm + kMaxNbk * (kMaxNbk + 1));
-  __shared__ double lp[kMaxNbk];
+  __shared__ double colb[2][kMaxNbk];
+  __shared__ double dpiv[kMaxNbk];
+  __shared__ double sq[kMaxNbk];
+  __shared__ T lsh[kMaxNbk][kMaxNbk + 1];
+  __shared__ T xrow[2][kMaxNbk];
   __shared__ int bad;
   const DiagTask tk = tasks[blockIdx.x];
   const int w = tk.w;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   T* blk = L + tk.a;
-  for (int e = tid; e < w * w; e += 256) {
-    int i = e / w, j = e % w;
-    a[i][j] = (j <= i) ? A(blk[int64_t(i) * tk.lda + j]) : A(0);
-    x[i][j] = (i == j) ? A(1) : A(0);
-  }
+  double r[4][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int i = ty + 16 * m, k = tx + 16 * n;
+      r[m][n] = (k <= i && i < w) ? double(blk[int64_t(i) * tk.lda + k]) : 0.0;
+    }
   if (tid == 0) bad = 0;
+  if (tx == 0) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+      if (ty + 16 * m < w) colb[0][ty + 16 * m] = r[m][0];
+  }
   __syncthreads();
   for (int j = 0; j < w; ++j) {
-    if (tid == 0) {
-      A d = a[j][j];
-      if (!(d > A(0)) || !isfinite(double(d))) { bad = 1; d = A(1); }
-      const A piv = sqrt(d);
-      a[j][j] = piv;
-      lp[j] = double(piv);
+    const double* c = colb[j & 1];
+    double d = c[j];
+    if (!(d > 0.0) || !isfinite(d)) {
+      d = 1.0;
+      if (tid == 0) bad = 1;
     }
-    __syncthreads();
-    const A inv = A(1) / a[j][j];
-    for (int e = tid; e < w; e += 256) {
-      if (e > j) a[e][j] *= inv;
-      if (e <= j) x[j][e] *= inv;
+    double q = 0.0;
+    if ((tid & 31) == 0) q = 1.0 / d;
+    const double dv = __shfl_sync(0xffffffffu, q, 0);
+    if (tid == 0) dpiv[j] = d;
+    double ci[4], ck[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = ty + 16 * m;
+      ci[m] = (i > j && i < w) ? c[i] * dv : 0.0;
     }
-    __syncthreads();
-    const int rem = w - j - 1;
-    // a[i][k] -= a[i][j] a[k][j] (j < k <= i), x[i][c] -= a[i][j] x[j][c] (c <= j)
-    for (int e = tid; e < rem * (rem + j + 1); e += 256) {
-      const int i = j + 1 + e / (rem + j + 1), q = e % (rem + j + 1);
-      const A lij = a[i][j];
-      if (q < rem) {
-        const int k = j + 1 + q;
-        if (k <= i) a[i][k] -= lij * a[k][j];
-      } else {
-        const int c = q - rem;
-        x[i][c] -= lij * x[j][c];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int k = tx + 16 * n;
+      ck[n] = (k > j && k < w) ? c[k] : 0.0;
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (16 * m + 15 <= j) continue;  // block row finished (uniform over the CTA)
+#pragma unroll
+      for (int n = 0; n <= m; ++n) {
+        if (16 * n + 15 <= j) continue;
+        r[m][n] -= ci[m] * ck[n];
+      }
+    }
+    // publish column j + 1 (its owners hold it fully reduced by columns 0..j)
+    const int jn = j + 1;
+    if (jn < w && tx == (jn & 15)) {
+      const int n = jn >> 4;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int i = ty + 16 * m;
+        if (i >= jn && i < w) {
+#pragma unroll
+          for (int nn = 0; nn < 4; ++nn)
+            if (nn == n) colb[jn & 1][i] = r[m][nn];
+        }
       }
     }
     __syncthreads();
   }
+  if (tid < w) sq[tid] = sqrt(dpiv[tid]);
   if (tid < 32) {
     double s = 0.0;
-    for (int j = tid; j < w; j += 32) s += log(lp[j]);
+    for (int j = tid; j < w; j += 32) s += 0.5 * log(dpiv[j]);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (tid == 0) {
       logpiv[blockIdx.x] = s;
       if (bad) atomicCAS(err, -1, tk.front);
     }
   }
-  T* dv = dinv + tk.dinv;
-  for (int e = tid; e < w * w; e += 256) {
-    int i = e / w, j = e % w;
-    blk[int64_t(i) * tk.lda + j] = T(j <= i ? a[i][j] : A(0));
-    dv[int64_t(i) * kMaxNbk + j] = T(j <= i ? x[i][j] : A(0));
+  __syncthreads();
+  // L = a_ik / sqrt(d_k) below the diagonal, sqrt(d_k) on it; zero above
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int i = ty + 16 * m, k = tx + 16 * n;
+      if (i < w && k < w) {
+        const T v = k < i ? T(r[m][n] / sq[k]) : (k == i ? T(sq[k]) : T(0));
+        lsh[i][k] = v;
+        blk[int64_t(i) * tk.lda + k] = v;
+      }
+    }
+  // X = L^-1: B = I; step j takes the finished row j of X and applies
+  // B_ic -= L_ij X_jc (i > j, c <= j); row j + 1 finishes as B_(j+1)c / L_(j+1)(j+1)
+  T b[4][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) b[m][n] = (ty + 16 * m == tx + 16 * n) ? T(1) : T(0);
+  __syncthreads();
+  if (ty == 0 && tx == 0) {
+    b[0][0] = T(1) / lsh[0][0];
+    xrow[0][0] = b[0][0];
   }
+  __syncthreads();
+  for (int j = 0; j < w; ++j) {
+    const T* xr = xrow[j & 1];
+    T li[4], xc[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = ty + 16 * m;
+      li[m] = (i > j && i < w) ? lsh[i][j] : T(0);
+    }
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int cc = tx + 16 * n;
+      xc[n] = cc <= j ? xr[cc] : T(0);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (16 * m + 15 <= j) continue;
+#pragma unroll
+      for (int n = 0; n <= m; ++n) {
+        if (16 * n > j) continue;  // columns beyond j of row j of X are zero
+        b[m][n] -= li[m] * xc[n];
+      }
+    }
+    const int jn = j + 1;
+    if (jn < w && ty == (jn & 15)) {
+      const int m = jn >> 4;
+      const T inv = T(1) / lsh[jn][jn];
+#pragma unroll
+      for (int mm = 0; mm < 4; ++mm) {
+        if (mm != m) continue;
+#pragma unroll
+        for (int n = 0; n < 4; ++n) {
+          const int cc = tx + 16 * n;
+          if (cc <= jn) {
+            b[mm][n] *= inv;
+            xrow[jn & 1][cc] = b[mm][n];
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  T* dv = dinv + tk.dinv;
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int i = ty + 16 * m, cc = tx + 16 * n;
+      if (i < w && cc < w) dv[int64_t(i) * kMaxNbk + cc] = cc <= i ? b[m][n] : T(0);
+    }
 }
 
 template <typename T>
 void launch_potrf(const DiagTask* tasks, int ntasks, T* L, T* dinv, double* logpiv, int* err, cudaStream_t st) {
   if (ntasks <= 0) return;
-  using Arith = double;  // FP64 arithmetic on both paths (the mixed path's pivots carry the log-determinant)
-  const int smem = 2 * kMaxNbk * (kMaxNbk + 1) * int(sizeof(Arith));
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(potrf_kernel<T, Arith>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr = true;
-  }
-  potrf_kernel<T, Arith><<<ntasks, 256, smem, st>>>(tasks, L, dinv, logpiv, err);
+  potrf_kernel<T><<<ntasks, 256, 0, st>>>(tasks, L, dinv, logpiv, err);
 }
 template void launch_potrf<double>(const DiagTask*, int, double*, double*, double*, int*, cudaStream_t);
 template void launch_potrf<float>(const DiagTask*, int, float*, float*, double*, int*, cudaStream_t);
