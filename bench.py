@@ -29,6 +29,36 @@ sys.path.insert(0, ROOT)
 METRIC = "logL+grad evals/s & samples/s, 200x200x24 SPDE: mixed+learned vs FP64 plain"
 
 
+# DRAM bytes per algorithmic flop of the tensor-core product, from the ncu
+# captures of its two largest launches at 100 x 100 x 24 (an inverse-block
+# product, 4.34e11 flops, and a Schur update, 2.27e11 flops): 2.131e9 bytes.
+TC_DRAM_BYTES_PER_FLOP = 2.131e9 / 6.605e11
+
+
+def _tf32_tflops(torch, n=8192, reps=10):
+    """cuBLAS FP32 GEMM with TF32 tensor cores allowed, best of `reps` (the
+    single-pass TF32 rate; a 3xTF32 product issues three such passes)."""
+    try:
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = True
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        torch.matmul(a, b)
+        best = 1e30
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        torch.backends.cuda.matmul.allow_tf32 = prev
+        del a, b
+        return 2.0 * n ** 3 / (best / 1e3) / 1e12
+    except Exception:
+        return None
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -205,7 +235,7 @@ def main():
     clk = clocks.stop()
     L.spde_plan_set_profiling(plan.h, 0)
     launches = plan.info().launches - launches0
-    pms, pfl, pct = (np.zeros(9), np.zeros(9), np.zeros(9, dtype=np.int64))
+    pms, pfl, pct = (np.zeros(10), np.zeros(10), np.zeros(10, dtype=np.int64))
     L.spde_plan_read_profile(plan.h, pms.ctypes.data, pfl.ctypes.data, pct.ctypes.data, 1)
     sms, sfl, stl = np.zeros(18), np.zeros(18), np.zeros(18, dtype=np.int64)
     L.spde_plan_read_sites(plan.h, sms.ctypes.data, sfl.ctypes.data, stl.ctypes.data, 1)
@@ -255,11 +285,13 @@ def main():
                 "rel_dgrad_mixed_vs_fp64": float(np.abs(jac - j64).max() / np.abs(j64).max())}
 
     peaks, peak_src = _peaks()
-    gemm_ms = pms[3] / args.steps
-    gemm_launch_avg_ms = pms[3] / max(1, pct[3])
-    gemm_flops_per_launch = pfl[3] / max(1, pct[3])
-    achieved = gemm_flops_per_launch / (gemm_launch_avg_ms / 1e3) / 1e12
+    # dominant kernel: the tensor-core tiled product (profile class 9)
+    tc_ms = pms[9] / args.steps
+    tc_launch_avg_ms = pms[9] / max(1, pct[9])
+    tc_flops_per_launch = pfl[9] / max(1, pct[9])
+    achieved = tc_flops_per_launch / (tc_launch_avg_ms / 1e3) / 1e12
     peak = float(peaks.get("bf16_tflops", 1900.0))
+    tf32 = _tf32_tflops(torch)
     if rank != 0:
         return
     cb = None if args.no_cpu else cpu_baseline()
@@ -276,13 +308,19 @@ def main():
                 "d2h_bytes_per_step": int(canon.size) * 8 + 8},
         "samples_per_s": samples_per_s,
         "gpu_launches": int(launches),
-        "roofline": {"bound": "tensor", "kernel": "tiled product (Schur update / trailing update / inverse blocks)",
+        "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel (3xTF32 tiled product: factor and inverse updates)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "peak_source": f"bf16 dense {peak_src}", "traffic": None,
-                     "share_of_step": gemm_ms / (ms / args.steps)},
+                     "peak_source": f"bf16 dense {peak_src}",
+                     "traffic": TC_DRAM_BYTES_PER_FLOP * tc_flops_per_launch,
+                     "traffic_source": "ncu dram bytes per flop of two captured launches (100x100x24), "
+                                       "scaled by this run's flops per launch",
+                     "launches_per_step": float(pct[9] / args.steps),
+                     "share_of_step": tc_ms / (ms / args.steps),
+                     "tf32_cublas_tflops": tf32,
+                     "frac_of_3xtf32": achieved / (tf32 / 3.0) if tf32 else None},
         "profile_ms_per_step": {k: float(pms[i] / args.steps) for i, k in enumerate(
-            ["memset", "extend_add", "diag_block", "tiled_product", "fwd_gather", "bwd_gather", "inv_gather",
-             "transpose", "inv_extract"])},
+            ["memset", "extend_add", "diag_block", "product_cuda_cores", "fwd_gather", "bwd_gather", "inv_gather",
+             "transpose", "inv_extract", "product_tensor_cores"])},
         "algorithmic": {"factor_tflop": info.factor_flops / 1e12, "selinv_tflop": info.selinv_flops / 1e12,
                         "nnz_L": info.nnz_l},
         "gemm_sites": sites,

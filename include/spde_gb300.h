@@ -94,10 +94,11 @@ int spde_plan_set_stream(SpdePlan* plan, void* stream);
 int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info);
 const char* spde_last_error(const SpdePlan* plan);
 /* Optional per-launch timing with CUDA events on the plan's stream (no
- * reference counterpart; measurement only).  read_profile fills 9 entries per
- * launch class (0 memset, 1 extend-add, 2 diagonal block, 3 tiled product,
- * 4 forward gather, 5 backward gather, 6 inverse gather, 7 transpose,
- * 8 inverse extraction): milliseconds, algorithmic flops, launches. */
+ * reference counterpart; measurement only).  read_profile fills 10 entries per
+ * launch class (0 memset, 1 extend-add, 2 diagonal block, 3 tiled product on
+ * the CUDA cores, 4 forward gather, 5 backward gather, 6 inverse gather,
+ * 7 transpose, 8 inverse extraction, 9 tiled product on the tensor cores):
+ * milliseconds, algorithmic flops, launches. */
 int spde_plan_set_profiling(SpdePlan* plan, int enable);
 int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* count, int reset);
 /* The same timing split by call site of the tiled product (18 entries: factor

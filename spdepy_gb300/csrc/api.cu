@@ -299,7 +299,7 @@ int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* c
   if (!plan) return SPDE_ERR_ARG;
   Plan& p = plan->p;
   prof_collect(&p);
-  for (int k = 0; k < 9; ++k) {
+  for (int k = 0; k < kProfClasses; ++k) {
     if (ms) ms[k] = p.prof_ms[k];
     if (flops) flops[k] = p.prof_flops[k];
     if (count) count[k] = p.prof_count[k];

@@ -822,6 +822,7 @@ struct Exec {
     cudaStream_t st = p->stream;
     for (const Op& o : s.ops) {
       const bool timed = p->profile && o.kind != OP_MEMSET;
+      const bool on_tc = o.kind == OP_GEMM && sizeof(T) == sizeof(float) && o.tc && tc_gemm_enabled();
       if (timed) prof_begin(p, st);
       switch (o.kind) {
         case OP_MEMSET: cudaMemsetAsync(buf(o.cbuf), 0, size_t(o.elems) * sizeof(T), st); break;
@@ -835,7 +836,7 @@ struct Exec {
         case OP_GEMM:
           launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st,
                          o.tc != 0);
-          if (sizeof(T) == sizeof(float) && o.tc && tc_gemm_enabled()) tc_launch_log(o);
+          if (on_tc) tc_launch_log(o);
           break;
         case OP_SGATHER_FWD: {
           int pd = o.depth & 1;
@@ -863,7 +864,7 @@ struct Exec {
                                                       p->sym.nslots, buf(o.cbuf), zq);
           break;
       }
-      if (timed) prof_end(p, st, o.kind, o.flops, o.site, o.kind == OP_GEMM ? o.count : 0);
+      if (timed) prof_end(p, st, on_tc ? kProfTensorCore : o.kind, o.flops, o.site, o.kind == OP_GEMM ? o.count : 0);
     }
     p->launches_total += s.launches;
   }

@@ -16,6 +16,9 @@ namespace spde {
 enum OpKind {
   OP_MEMSET = 0, OP_EXTEND, OP_DIAG, OP_GEMM, OP_SGATHER_FWD, OP_SGATHER_BWD, OP_ZGATHER, OP_MIRROR, OP_ZEXTRACT
 };
+// profile class of a tiled product that ran on the tensor cores (the others count as OP_GEMM)
+constexpr int kProfTensorCore = 9;
+constexpr int kProfClasses = 10;
 enum BufId { B_NONE = 0, B_L, B_DINV, B_P0, B_P1, B_X, B_W0, B_W1, B_G0, B_G1, B_SX };
 
 // Call sites of the tiled product (for per-site timing).
