@@ -31,6 +31,12 @@ extern "C" {
 
 #define SPDE_PRECISION_FP64 0 /* factor, solves and inverse in FP64 */
 #define SPDE_PRECISION_MIXED 1 /* FP32 factor, FP64 pivots / log-det / refinement */
+#define SPDE_PRECISION_ITERATIVE 2 /* no factorisation: assembly, products, PCG */
+
+#define SPDE_PRECOND_NONE 0
+#define SPDE_PRECOND_JACOBI 1
+#define SPDE_PRECOND_LEARNED 2
+#define SPDE_PRECOND_NPARAMS 3323
 
 typedef struct SpdePlan SpdePlan;
 
@@ -87,7 +93,10 @@ int spde_advection_triplets(int M, int N, const double* G, const double* dG, int
                             int diff, int* row, int* col, double* val, void* stream);
 
 /* ---- plan: symbolic analysis + device arenas (the analysis half of
- * sksparse.cholmod.cholesky, called at spdes/advection_diffusion2D.py:117,193). */
+ * sksparse.cholmod.cholesky, called at spdes/advection_diffusion2D.py:117,193).
+ * precision SPDE_PRECISION_ITERATIVE makes a plan without ordering or factor
+ * arenas (assembly, products and PCG only); factor-based calls then return
+ * SPDE_ERR_STATE. */
 int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out);
 int spde_plan_destroy(SpdePlan* plan);
 int spde_plan_set_stream(SpdePlan* plan, void* stream);
@@ -166,6 +175,38 @@ int spde_loglike(SpdePlan* plan, const double* theta_host, int ntheta, const dou
 /* Conditional mean mu = mu0 + tau (Q + tau S^T S)^-1 S^T (y - S mu0) (model.py:120-127);
  * y_dev m values, mu0_dev/mu_dev n values (device FP64). */
 int spde_conditional_mean(SpdePlan* plan, double tau, const double* y_dev, const double* mu0_dev, double* mu_dev);
+
+/* ---- learned preconditioner and PCG (no reference counterpart: the reference
+ * factors every system with CHOLMOD; these serve grids too large to factor).
+ * M^-1 = G^T G with G a 27-point space-time stencil whose weights a small
+ * network computes from each node's normalised row of A = Q (+ tau S^T S).
+ * Network parameters: SPDE_PRECOND_NPARAMS FP32 values in device memory
+ * (layout W1[32][42], b1[32], W2[32][32], b2[32], W3[27][32], b3[27]). */
+int spde_precond_nparams(void);
+/* G weights (n x 27, FP32, device) for the assembled model; act_dev (optional,
+ * n x 107 FP32) keeps the activations a gradient step needs. */
+int spde_precond_weights(SpdePlan* plan, int with_obs, double tau, const float* params_dev, float* w_dev,
+                         float* act_dev);
+/* Training loss ||z - G A G^T z||^2 / (n k) for the probe block z_dev (n x k,
+ * row-major, FP64) and its gradient with respect to the parameters (grad_dev,
+ * SPDE_PRECOND_NPARAMS FP32). */
+int spde_precond_grad(SpdePlan* plan, int with_obs, double tau, const float* params_dev, const float* w_dev,
+                      const float* act_dev, const double* z_dev, int k, double* loss, float* grad_dev);
+/* One Adam update of n parameters on the plan's stream (step t >= 1). */
+int spde_adam_step(SpdePlan* plan, float* params_dev, const float* grad_dev, float* m_dev, float* v_dev, int n,
+                   double lr, double b1, double b2, double eps, int t);
+/* z <- (I - omega D^-1 A)^sweeps z, then every column scaled to unit RMS
+ * (z_dev n x nrhs, FP64): the error a damped-Jacobi sweep leaves after
+ * `sweeps` steps from z, i.e. the smooth residual directions CG has to work on;
+ * used as training probes. */
+int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, int sweeps, double* z_dev, int nrhs);
+/* x = A^-1 b by preconditioned CG (x from 0), nrhs columns row-major, FP64
+ * device; precond SPDE_PRECOND_* (w_dev: G weights for LEARNED).  Stops when
+ * every column reaches ||b - A x|| <= tol ||b|| (checked every 8 iterations) or
+ * after maxit iterations; *relres is the worst true relative residual.
+ * Returns SPDE_ERR_NOT_CONVERGED when the tolerance was not reached. */
+int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float* w_dev, const double* b_dev,
+             double* x_dev, int nrhs, double tol, int maxit, int* iters, double* relres);
 
 #ifdef __cplusplus
 }

@@ -11,7 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libspde_gb300.so")
-SOURCES = ["symbolic.cpp", "dense.cu", "tc_gemm.cu", "assemble.cu", "engine.cu", "adjoint.cu", "api.cu"]
+SOURCES = ["symbolic.cpp", "dense.cu", "tc_gemm.cu", "assemble.cu", "engine.cu", "adjoint.cu", "pcg.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

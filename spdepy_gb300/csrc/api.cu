@@ -25,6 +25,9 @@ using namespace spde;
 
 namespace {
 
+// relative residual the FP64 refinement of the conditional-mean solve stops at
+constexpr double kRefineTol = 1e-10;
+
 __global__ void obs_rhs_kernel(const int* __restrict__ idx, int m, int r, double tau, const double* __restrict__ y,
                                const double* __restrict__ mu0, double* __restrict__ b) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -216,12 +219,28 @@ int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int
   return SPDE_OK;
 }
 
+static int no_factor(SpdePlan* plan) {
+  plan->p.last_error = "this plan was created for iterative solves only (no factorisation)";
+  return SPDE_ERR_STATE;
+}
+
 int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out) {
-  if (!out || (precision != 0 && precision != 1)) return SPDE_ERR_ARG;
+  if (!out || precision < 0 || precision > 2) return SPDE_ERR_ARG;
   *out = nullptr;
   SpdePlan* plan = new (std::nothrow) SpdePlan();
   if (!plan) return SPDE_ERR_NO_MEMORY;
   plan->p.precision = precision;
+  if (precision == SPDE_PRECISION_ITERATIVE) {
+    // assembly, products and iterative solves only: no ordering, no factor arenas
+    if (Mx < 3 || Ny < 3 || T < 1 || int64_t(Mx) * Ny * T > (int64_t(1) << 31) - 1) {
+      delete plan;
+      return SPDE_ERR_ARG;
+    }
+    Symbolic& S = plan->p.sym;
+    S.Mx = Mx; S.Ny = Ny; S.T = T; S.n = Mx * Ny * T; S.nslots = T == 1 ? 25 : 43;
+    *out = plan;
+    return SPDE_OK;
+  }
   if (build_symbolic(Mx, Ny, T, leaf_max > 0 ? leaf_max : 128, 64, &plan->p.sym) != 0) {
     delete plan;
     return SPDE_ERR_ARG;
@@ -246,6 +265,7 @@ int spde_plan_destroy(SpdePlan* plan) {
   for (void* q : ptrs) cudaFree(q);
   cudaFree(p.d_part);
   cudaFree(p.d_sx);
+  cudaFree(p.d_pc);
   for (cudaEvent_t e : p.ev_pool) cudaEventDestroy(e);
   p.sched_factor.release();
   p.sched_selinv.release();
@@ -417,6 +437,7 @@ int spde_set_obs(SpdePlan* plan, const int64_t* idx, int m) {
 }
 
 int spde_factor(SpdePlan* plan, int with_obs, double tau, double* logdet) {
+  if (plan && plan->p.precision == SPDE_PRECISION_ITERATIVE) return no_factor(plan);
   if (!plan) return SPDE_ERR_ARG;
   int rc = plan_factor(&plan->p, with_obs, tau);
   if (rc == 0 && logdet) *logdet = plan->p.logdet;
@@ -424,16 +445,19 @@ int spde_factor(SpdePlan* plan, int with_obs, double tau, double* logdet) {
 }
 
 int spde_solve(SpdePlan* plan, const double* b, double* x, int nrhs, int iters, double tol, double* resid) {
+  if (plan && plan->p.precision == SPDE_PRECISION_ITERATIVE) return no_factor(plan);
   if (!plan || !b || !x) return SPDE_ERR_ARG;
   return plan_solve(&plan->p, b, x, nrhs, iters, tol, resid);
 }
 
 int spde_sample(SpdePlan* plan, const double* z, double* x, int nrhs) {
+  if (plan && plan->p.precision == SPDE_PRECISION_ITERATIVE) return no_factor(plan);
   if (!plan || !z || !x || nrhs < 1) return SPDE_ERR_ARG;
   return plan_sample(&plan->p, z, x, nrhs);
 }
 
 int spde_selinv(SpdePlan* plan, double* zq) {
+  if (plan && plan->p.precision == SPDE_PRECISION_ITERATIVE) return no_factor(plan);
   if (!plan || !zq) return SPDE_ERR_ARG;
   return plan_selinv(&plan->p, zq);
 }
@@ -477,6 +501,7 @@ int spde_adjoint_noalloc(SpdePlan* plan, const double* gbar, double* grad_dev) {
 }
 
 int spde_conditional_mean(SpdePlan* plan, double tau, const double* y, const double* mu0, double* mu) {
+  if (plan && plan->p.precision == SPDE_PRECISION_ITERATIVE) return no_factor(plan);
   if (!plan || !y || !mu) return SPDE_ERR_ARG;
   Plan& p = plan->p;
   if (!p.d_obs_idx) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
@@ -487,7 +512,7 @@ int spde_conditional_mean(SpdePlan* plan, double tau, const double* y, const dou
   API_CUDA(cudaMemsetAsync(b, 0, size_t(p.sym.n) * sizeof(double), p.stream));
   obs_rhs_kernel<<<(p.nobs + 255) / 256 + 1, 256, 0, p.stream>>>(p.d_obs_idx, p.nobs, 1, tau, y, mu0, b);
   double resid = 0.0;
-  rc = plan_solve(&p, b, mu, 1, p.precision == 0 ? 1 : 10, 1e-12, &resid);
+  rc = plan_solve(&p, b, mu, 1, p.precision == 0 ? 1 : 10, kRefineTol, &resid);
   if (rc == 0 && mu0) {
     // mu += mu0, written as mu - (0 - mu0) with the subtraction kernel
     API_CUDA(cudaMemsetAsync(b, 0, size_t(p.sym.n) * sizeof(double), p.stream));
@@ -501,6 +526,7 @@ int spde_conditional_mean(SpdePlan* plan, double tau, const double* y, const dou
 
 int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* y, int r, int grad_mode,
                  const double* V, int nh1, double* f_out, double* jac) {
+  if (plan && plan->p.precision == SPDE_PRECISION_ITERATIVE) return no_factor(plan);
   if (!plan || !theta || !y || r < 1 || !f_out || grad_mode < 0 || grad_mode > 2) return SPDE_ERR_ARG;
   Plan& p = plan->p;
   if (!p.d_obs_idx || p.nobs < 1) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
@@ -518,7 +544,7 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   if (exact) { API_CUDA(S.zq.ensure(size_t(n) * ns)); API_CUDA(S.zqc.ensure(size_t(n) * ns)); }
   if (hutch) { API_CUDA(S.trq.ensure(size_t(n) * nh1)); API_CUDA(S.trc.ensure(size_t(n) * nh1)); }
   const int iters = p.precision == 0 ? 1 : 10;
-  const double tol = 1e-12;
+  const double tol = kRefineTol;
   // Q: log-determinant, then its inverse on the pattern (or Hutchinson solves)
   double ldq = 0.0, ldqc = 0.0, res = 0.0;
   if ((rc = plan_factor(&p, 0, 0.0))) return rc;
@@ -575,4 +601,59 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   return SPDE_OK;
 }
 
+// ------------------------------------------------------------ learned PCG
+int spde_precond_nparams(void) { return kPcParams; }
+
+int spde_precond_weights(SpdePlan* plan, int with_obs, double tau, const float* params, float* w, float* act) {
+  if (!plan || !params || !w) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  return pc_weights(&p, with_obs, tau, params, w, act) ? SPDE_ERR_CUDA : SPDE_OK;
+}
+
+int spde_precond_grad(SpdePlan* plan, int with_obs, double tau, const float* params, const float* w,
+                      const float* act, const double* z, int k, double* loss, float* grad) {
+  if (!plan || !params || !w || !act || !z || k < 1 || !loss || !grad) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  const int rc = pc_grad(&p, with_obs, tau, params, w, act, z, k, loss, grad);
+  if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+  return rc ? SPDE_ERR_CUDA : SPDE_OK;
+}
+
+int spde_adam_step(SpdePlan* plan, float* params, const float* grad, float* m, float* v, int n, double lr, double b1,
+                   double b2, double eps, int t) {
+  if (!plan || !params || !grad || !m || !v || n < 1 || t < 1) return SPDE_ERR_ARG;
+  return pc_adam(grad, params, m, v, n, float(lr), float(b1), float(b2), float(eps), t, plan->p.stream)
+             ? SPDE_ERR_CUDA
+             : SPDE_OK;
+}
+
+int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, int sweeps, double* z, int nrhs) {
+  if (!plan || !z || nrhs < 1 || sweeps < 0) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  const int rc = jacobi_smooth(&p, with_obs, tau, omega, sweeps, z, nrhs);
+  if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+  return rc ? SPDE_ERR_CUDA : SPDE_OK;
+}
+
+int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float* w, const double* b, double* x,
+             int nrhs, double tol, int maxit, int* iters, double* relres) {
+  if (!plan || !b || !x || nrhs < 1 || maxit < 1 || !iters || !relres || precond < 0 || precond > 2 ||
+      (precond == 2 && !w))
+    return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  const int rc = pcg_solve(&p, with_obs, tau, precond, w, b, x, nrhs, tol, maxit, 8, iters, relres);
+  if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+  if (rc == 6) { p.last_error = "PCG did not reach the tolerance"; return SPDE_ERR_NOT_CONVERGED; }
+  return rc ? SPDE_ERR_CUDA : SPDE_OK;
+}
+
 }  // extern "C"
+

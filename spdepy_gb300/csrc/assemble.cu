@@ -163,22 +163,6 @@ __global__ void qstencil_kernel(DevModel m, const double* __restrict__ Ageo, con
   cQs[c] = cfac * qs[c];
 }
 
-// Value of Q at node (cell c, time t), stencil offset (dx, dy, dt).
-__device__ __forceinline__ double qval(const QStencil& q, int c, int t, int dx, int dy, int dt) {
-  if (q.T == 1) return q.QA[int64_t(c) * 25 + (dy + 2) * 5 + dx + 2];
-  if (dt == 0) {
-    const int s = (dy + 2) * 5 + dx + 2;
-    const bool ctr = dx == 0 && dy == 0;
-    if (t == 0) return q.Q0[int64_t(c) * 25 + s] + (ctr ? q.cQs[c] : 0.0);
-    double v = q.QA[int64_t(c) * 25 + s];
-    if (t < q.T - 1 && ctr) v += q.cQs[c];
-    return v;
-  }
-  if (dt == 1) return q.QO[int64_t(c) * 9 + (dy + 1) * 3 + dx + 1];
-  const int mcell = c + dy * q.Mx + dx;
-  return q.QO[int64_t(mcell) * 9 + (1 - dy) * 3 + (1 - dx)];
-}
-
 __device__ __forceinline__ void slot_off(int T, int s, int* dx, int* dy, int* dt) {
   if (T == 1) { *dt = 0; *dy = s / 5 - 2; *dx = s % 5 - 2; return; }
   if (s < 9) { *dt = -1; *dy = s / 3 - 1; *dx = s % 3 - 1; }
@@ -223,29 +207,6 @@ __global__ void scatter_kernel(QStencil q, int nslots, const int* __restrict__ a
   if (obs_cnt && dx == 0 && dy == 0 && dt == 0) v += tau * obs_cnt[k];
   const DevFront f = fronts[front_of[perm[k]]];
   L[f.p_off + off] = T(v);
-}
-
-// y = (Q + tau S^T S) x for nrhs columns, natural order, FP64.
-__global__ void spmv_kernel(QStencil q, const int* __restrict__ obs_cnt, double tau, const double* __restrict__ x,
-                            double* __restrict__ y, int nrhs) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int64_t n = int64_t(q.Ns) * q.T;
-  if (e >= n * nrhs) return;
-  const int k = int(e / nrhs), r = int(e % nrhs);
-  const int t = k / q.Ns, c = k - t * q.Ns;
-  const int yy = c / q.Mx, xx = c - yy * q.Mx;
-  const int ns = q.T == 1 ? 25 : 43;
-  double acc = 0.0;
-  for (int s = 0; s < ns; ++s) {
-    int dx, dy, dt;
-    slot_off(q.T, s, &dx, &dy, &dt);
-    int x2 = xx + dx, y2 = yy + dy, t2 = t + dt;
-    if (x2 < 0 || x2 >= q.Mx || y2 < 0 || y2 >= q.Ny || t2 < 0 || t2 >= q.T) continue;
-    int64_t nb = (int64_t(t2) * q.Ny + y2) * q.Mx + x2;
-    acc = fma(qval(q, c, t, dx, dy, dt), x[nb * nrhs + r], acc);
-  }
-  if (obs_cnt) acc = fma(tau * obs_cnt[k], x[int64_t(k) * nrhs + r], acc);
-  y[e] = acc;
 }
 
 // ---------------------------------------------------- stencil triplets (B3)
@@ -330,10 +291,80 @@ template void launch_scatter<double>(const QStencil&, int, const int*, const int
                                      const int*, double, double*, cudaStream_t);
 template void launch_scatter<float>(const QStencil&, int, const int*, const int*, const int*, const DevFront*,
                                     const int*, double, float*, cudaStream_t);
+// y = (Q + tau S^T S) x with one thread per (spatial cell, column) sweeping the
+// time axis: the cell's time-invariant coefficients (25 in-block values, 9 to
+// t + 1 and the 9 mirrored from the neighbours to t - 1) are loaded once and
+// reused for all T blocks.
+__global__ void __launch_bounds__(128) spmv_cells_kernel(QStencil q, const int* __restrict__ obs, double tau,
+                                                         const double* __restrict__ x, double* __restrict__ y,
+                                                         int nrhs) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(q.Ns) * nrhs) return;
+  const int c = int(e / nrhs), r = int(e - int64_t(c) * nrhs);
+  const int cy = c / q.Mx, cx = c - cy * q.Mx;
+  double qa[25], qf[9], qb[9];
+  uint32_t m25 = 0, m9 = 0;
+#pragma unroll
+  for (int s = 0; s < 25; ++s) {
+    const int dx = s % 5 - 2, dy = s / 5 - 2;
+    const bool in = cx + dx >= 0 && cx + dx < q.Mx && cy + dy >= 0 && cy + dy < q.Ny;
+    m25 |= uint32_t(in) << s;
+    qa[s] = q.QA[int64_t(c) * 25 + s];
+  }
+  if (q.T > 1) {
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+      const int dx = s % 3 - 1, dy = s / 3 - 1;
+      const bool in = cx + dx >= 0 && cx + dx < q.Mx && cy + dy >= 0 && cy + dy < q.Ny;
+      m9 |= uint32_t(in) << s;
+      qf[s] = q.QO[int64_t(c) * 9 + s];
+      qb[s] = in ? q.QO[int64_t(c + dy * q.Mx + dx) * 9 + (8 - s)] : 0.0;
+    }
+  }
+  const double cqs = q.T > 1 ? q.cQs[c] : 0.0;
+  for (int t = 0; t < q.T; ++t) {
+    const int64_t k = int64_t(t) * q.Ns + c;
+    const double* xt = x + k * nrhs + r;
+    double acc = 0.0;
+    if (t == 0 && q.T > 1) {
+#pragma unroll
+      for (int s = 0; s < 25; ++s)
+        if (m25 >> s & 1u) {
+          const int off = (s / 5 - 2) * q.Mx + (s % 5 - 2);
+          acc = fma(q.Q0[int64_t(c) * 25 + s], xt[int64_t(off) * nrhs], acc);
+        }
+    } else {
+#pragma unroll
+      for (int s = 0; s < 25; ++s)
+        if (m25 >> s & 1u) {
+          const int off = (s / 5 - 2) * q.Mx + (s % 5 - 2);
+          acc = fma(qa[s], xt[int64_t(off) * nrhs], acc);
+        }
+    }
+    if (q.T > 1) {
+      if (t < q.T - 1 || t == 0) acc = fma(cqs, xt[0], acc);
+      if (t + 1 < q.T) {
+        const double* xn = xt + int64_t(q.Ns) * nrhs;
+#pragma unroll
+        for (int s = 0; s < 9; ++s)
+          if (m9 >> s & 1u) acc = fma(qf[s], xn[int64_t((s / 3 - 1) * q.Mx + (s % 3 - 1)) * nrhs], acc);
+      }
+      if (t > 0) {
+        const double* xp = xt - int64_t(q.Ns) * nrhs;
+#pragma unroll
+        for (int s = 0; s < 9; ++s)
+          if (m9 >> s & 1u) acc = fma(qb[s], xp[int64_t((s / 3 - 1) * q.Mx + (s % 3 - 1)) * nrhs], acc);
+      }
+    }
+    if (obs) acc = fma(tau * obs[k], xt[0], acc);
+    y[k * nrhs + r] = acc;
+  }
+}
+
 void launch_spmv(const QStencil& q, const int* obs, double tau, const double* x, double* y, int nrhs,
                  cudaStream_t st) {
-  int64_t tot = int64_t(q.Ns) * q.T * nrhs;
-  spmv_kernel<<<nblk(tot, 256), 256, 0, st>>>(q, obs, tau, x, y, nrhs);
+  const int64_t tot = int64_t(q.Ns) * nrhs;
+  spmv_cells_kernel<<<nblk(tot, 128), 128, 0, st>>>(q, obs, tau, x, y, nrhs);
 }
 void launch_diffusion_triplets(int M, int N, const double* H, int field, double hx, double hy, int bc, int* row,
                                int* col, double* val, cudaStream_t st) {

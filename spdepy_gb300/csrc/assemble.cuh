@@ -36,6 +36,24 @@ struct QStencil {
   int Mx, Ny, T, Ns;
 };
 
+#ifdef __CUDACC__
+// Value of Q at node (cell c, time t), stencil offset (dx, dy, dt).
+__device__ __forceinline__ double qval(const QStencil& q, int c, int t, int dx, int dy, int dt) {
+  if (q.T == 1) return q.QA[int64_t(c) * 25 + (dy + 2) * 5 + dx + 2];
+  if (dt == 0) {
+    const int s = (dy + 2) * 5 + dx + 2;
+    const bool ctr = dx == 0 && dy == 0;
+    if (t == 0) return q.Q0[int64_t(c) * 25 + s] + (ctr ? q.cQs[c] : 0.0);
+    double v = q.QA[int64_t(c) * 25 + s];
+    if (t < q.T - 1 && ctr) v += q.cQs[c];
+    return v;
+  }
+  if (dt == 1) return q.QO[int64_t(c) * 9 + (dy + 1) * 3 + dx + 1];
+  const int mcell = c + dy * q.Mx + dx;
+  return q.QO[int64_t(mcell) * 9 + (1 - dy) * 3 + (1 - dx)];
+}
+#endif
+
 void launch_fields(const DevModel& m, double* Ageo, double* A0geo, double* kap, double* qs, cudaStream_t st);
 void launch_qstencil(const DevModel& m, const double* Ageo, const double* A0geo, const double* kap, const double* qs,
                      double* Q0, double* QA, double* QO, double* cQs, double cfac, cudaStream_t st);

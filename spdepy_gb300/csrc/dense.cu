@@ -103,6 +103,100 @@ static void gemm_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, in
   else gemm_kernel<T, MODE, kCol, kCol><<<n, 256, 0, st>>>(t, A, B, C);
 }
 
+// ------------------------------------------------------------ narrow GEMM
+// Products with at most kNarrowN output columns (solves with few right-hand
+// sides) are bandwidth work: one CTA per task streams its (<= 128) A rows once,
+// coalesced, against B staged in shared memory, instead of computing a mostly
+// empty 128 x 128 register tile.  The block reads all of its A and B before it
+// writes C (in-place solves stay valid).
+constexpr int kNarrowN = 8;
+constexpr int kNarrowSmem = 24 * 1024;  // staged B (k x 8 columns) per chunk
+
+template <typename T, int MODE, int AL, int BL>
+__global__ void __launch_bounds__(256) gemv_kernel(const GemmTask* __restrict__ tasks, const T* Ab, const T* Bb,
+                                                   T* Cb) {
+  constexpr int kBEnt = kNarrowSmem / int(sizeof(T));  // staged B entries (k x n)
+  __shared__ T Bs[kBEnt];
+  __shared__ T acc_s[2][128][kNarrowN];
+  const GemmTask tk = tasks[blockIdx.x];
+  const T* A = Ab + tk.a;
+  const T* B = Bb + tk.b;
+  T* C = Cb + tk.c;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n = tk.n, m = tk.m;
+  const int kc = kBEnt / kNarrowN;  // k values per chunk
+  T s[kNarrowN];
+#pragma unroll
+  for (int j = 0; j < kNarrowN; ++j) s[j] = T(0);
+  for (int e = tid; e < 2 * 128 * kNarrowN; e += 256) (&acc_s[0][0][0])[e] = T(0);
+  for (int k0 = 0; k0 < tk.k; k0 += kc) {
+    const int kn = min(kc, tk.k - k0);
+    __syncthreads();
+    for (int e = tid; e < kn * n; e += 256) {
+      int kk, j;
+      if (BL == kRow) { j = e / kn; kk = e - j * kn; } else { kk = e / n; j = e - kk * n; }
+      Bs[kk * kNarrowN + j] = BL == kRow ? B[int64_t(j) * tk.ldb + k0 + kk] : B[int64_t(k0 + kk) * tk.ldb + j];
+    }
+    __syncthreads();
+    if (AL == kRow) {
+      // warp w owns rows w, w + 8, ...; lanes stride along the row
+      for (int i = warp; i < m; i += 8) {
+        T p[kNarrowN];
+#pragma unroll
+        for (int j = 0; j < kNarrowN; ++j) p[j] = T(0);
+        const T* ar = A + int64_t(i) * tk.lda + k0;
+        for (int kk = lane; kk < kn; kk += 32) {
+          const T a = ar[kk];
+#pragma unroll
+          for (int j = 0; j < kNarrowN; ++j)
+            if (j < n) p[j] = fma(a, Bs[kk * kNarrowN + j], p[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < kNarrowN; ++j) {
+          if (j >= n) break;
+          T v = p[j];
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+          if (lane == 0) acc_s[0][i][j] += v;
+        }
+      }
+    } else {
+      // thread (h, i): row i, every other k starting at h
+      const int i = tid & 127, h = tid >> 7;
+      if (i < m) {
+        for (int kk = h; kk < kn; kk += 2) {
+          const T a = A[int64_t(k0 + kk) * tk.lda + i];
+#pragma unroll
+          for (int j = 0; j < kNarrowN; ++j)
+            if (j < n) s[j] = fma(a, Bs[kk * kNarrowN + j], s[j]);
+        }
+      }
+    }
+  }
+  if (AL == kCol) {
+    const int i = tid & 127, h = tid >> 7;
+#pragma unroll
+    for (int j = 0; j < kNarrowN; ++j) acc_s[h][i][j] = s[j];
+  }
+  __syncthreads();
+  for (int e = tid; e < m * n; e += 256) {
+    const int i = e / n, j = e - i * n;
+    const T v = AL == kCol ? acc_s[0][i][j] + acc_s[1][i][j] : acc_s[0][i][j];
+    T* dst = C + int64_t(i) * tk.ldc + j;
+    if (MODE == kSub) *dst -= v;
+    else if (MODE == kStore) *dst = v;
+    else if (MODE == kNegStore) *dst = -v;
+    else *dst += v;
+  }
+}
+
+template <typename T, int MODE>
+static void gemv_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, int al, int bl, cudaStream_t st) {
+  if (al == kRow && bl == kRow) gemv_kernel<T, MODE, kRow, kRow><<<n, 256, 0, st>>>(t, A, B, C);
+  else if (al == kRow && bl == kCol) gemv_kernel<T, MODE, kRow, kCol><<<n, 256, 0, st>>>(t, A, B, C);
+  else if (al == kCol && bl == kRow) gemv_kernel<T, MODE, kCol, kRow><<<n, 256, 0, st>>>(t, A, B, C);
+  else gemv_kernel<T, MODE, kCol, kCol><<<n, 256, 0, st>>>(t, A, B, C);
+}
+
 // The FP32 products run on the tensor cores unless SPDE_TC=0 is set in the environment.
 bool tc_gemm_enabled() {
   static int on = -1;
@@ -115,10 +209,19 @@ bool tc_gemm_enabled() {
 
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout, int blayout,
-                 cudaStream_t st, bool tensor_cores) {
+                 cudaStream_t st, int path) {
   if (ntasks <= 0) return;
+  if (path == kPathNarrow) {
+    switch (mode) {
+      case kSub: gemv_mode<T, kSub>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+      case kStore: gemv_mode<T, kStore>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+      case kNegStore: gemv_mode<T, kNegStore>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+      default: gemv_mode<T, kAdd>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+    }
+    return;
+  }
   if constexpr (sizeof(T) == sizeof(float)) {
-    if (tensor_cores && tc_gemm_enabled()) {
+    if (path == kPathTensor && tc_gemm_enabled()) {
       launch_gemm_tc(tasks, ntasks, reinterpret_cast<const float*>(A), reinterpret_cast<const float*>(B),
                      reinterpret_cast<float*>(C), mode, alayout, blayout, st);
       return;
@@ -133,9 +236,9 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
 }
 
 template void launch_gemm<double>(const GemmTask*, int, const double*, const double*, double*, int, int, int,
-                                  cudaStream_t, bool);
+                                  cudaStream_t, int);
 template void launch_gemm<float>(const GemmTask*, int, const float*, const float*, float*, int, int, int,
-                                 cudaStream_t, bool);
+                                 cudaStream_t, int);
 
 // --------------------------------------------------- diagonal block POTRF
 // Cholesky factor and inverse of one w x w diagonal block (w <= 64) per CTA.

@@ -85,6 +85,12 @@ struct Builder {
   void split_by_k() {
     Op& o = s.ops.back();
     const int64_t beg = o.off, end = int64_t(s.gemm.size());
+    bool narrow = end > beg;
+    for (int64_t i = beg; i < end && narrow; ++i) narrow = s.gemm[i].n <= kNarrowMaxN;
+    if (narrow) {
+      o.tc = kPathNarrow;
+      return;
+    }
     auto mid = std::stable_partition(s.gemm.begin() + beg, s.gemm.begin() + end,
                                      [](const GemmTask& t) { return t.k >= kTcMinK; });
     const int64_t nlong = int64_t(mid - s.gemm.begin()) - beg;
@@ -822,7 +828,7 @@ struct Exec {
     cudaStream_t st = p->stream;
     for (const Op& o : s.ops) {
       const bool timed = p->profile && o.kind != OP_MEMSET;
-      const bool on_tc = o.kind == OP_GEMM && sizeof(T) == sizeof(float) && o.tc && tc_gemm_enabled();
+      const bool on_tc = o.kind == OP_GEMM && sizeof(T) == sizeof(float) && o.tc == kPathTensor && tc_gemm_enabled();
       if (timed) prof_begin(p, st);
       switch (o.kind) {
         case OP_MEMSET: cudaMemsetAsync(buf(o.cbuf), 0, size_t(o.elems) * sizeof(T), st); break;
@@ -835,7 +841,7 @@ struct Exec {
           break;
         case OP_GEMM:
           launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st,
-                         o.tc != 0);
+                         o.tc);
           if (on_tc) tc_launch_log(o);
           break;
         case OP_SGATHER_FWD: {

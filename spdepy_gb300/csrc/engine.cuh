@@ -19,6 +19,11 @@ enum OpKind {
 // profile class of a tiled product that ran on the tensor cores (the others count as OP_GEMM)
 constexpr int kProfTensorCore = 9;
 constexpr int kProfClasses = 10;
+
+// learned preconditioner (pcg.cu): 42 features, two hidden layers of 32, 27 stencil weights
+constexpr int kPcFeat = 42, kPcHidden = 32, kPcOffsets = 27;
+constexpr int kPcParams = kPcHidden * kPcFeat + kPcHidden + kPcHidden * kPcHidden + kPcHidden +
+                          kPcOffsets * kPcHidden + kPcOffsets;
 enum BufId { B_NONE = 0, B_L, B_DINV, B_P0, B_P1, B_X, B_W0, B_W1, B_G0, B_G1, B_SX };
 
 // Call sites of the tiled product (for per-site timing).
@@ -30,7 +35,7 @@ enum GemmSite {
 struct Op {
   double flops = 0.0;  // algorithmic flops of a GEMM launch (2 m n k summed over its tiles)
   int site = 0;
-  int tc = 1;          // FP32 products: 1 = tensor-core kernel, 0 = SIMT kernel
+  int tc = 1;          // product path (GemmPath): CUDA-core tiles, tensor-core tiles (FP32), narrow
   int kind = 0;
   int64_t off = 0;  // first task in the array of this kind
   int count = 0;
@@ -130,6 +135,9 @@ struct Plan {
   int64_t site_tiles[S_COUNT] = {0};
   std::vector<int> ev_site;
   std::string last_error;
+  // iterative solver / preconditioner scratch (pcg.cu)
+  void* d_pc = nullptr;
+  size_t pc_cap = 0;
 
   QStencil qstencil() const {
     QStencil q;
@@ -147,6 +155,16 @@ int plan_solve(Plan* p, const double* b_dev, double* x_dev, int nrhs, int refine
 int plan_selinv(Plan* p, double* zq_dev);
 int plan_sample(Plan* p, const double* z_dev, double* x_dev, int nrhs);
 void prof_collect(Plan* p);
+
+// learned preconditioner and PCG (pcg.cu)
+int pc_weights(Plan* p, int with_obs, double tau, const float* prm, float* w, float* act);
+int pc_grad(Plan* p, int with_obs, double tau, const float* prm, const float* w, const float* act, const double* z,
+            int k, double* loss, float* grad);
+int pc_adam(const float* g, float* prm, float* m, float* v, int n, float lr, float b1, float b2, float eps, int t,
+            cudaStream_t st);
+int jacobi_smooth(Plan* p, int with_obs, double tau, double omega, int sweeps, double* z, int nrhs);
+int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const double* b, double* x, int nrhs,
+              double tol, int maxit, int check_every, int* iters, double* relres);
 
 // adjoint (adjoint.cu)
 void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st);

@@ -41,9 +41,13 @@ struct DevFront {
   int child[2];
 };
 
+// product paths: CUDA-core tiles, tensor-core tiles (FP32 only), narrow (n <= 8 columns)
+enum GemmPath { kPathSimt = 0, kPathTensor = 1, kPathNarrow = 2 };
+constexpr int kNarrowMaxN = 8;
+
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout,
-                 int blayout, cudaStream_t st, bool tensor_cores = true);
+                 int blayout, cudaStream_t st, int path = kPathTensor);
 
 // tcgen05 path for FP32 (tc_gemm.cu); tc_gemm_take_error returns and clears the
 // bounded-wait error flag of that kernel.

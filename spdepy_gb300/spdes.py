@@ -39,7 +39,7 @@ MODEL_IDS = {1: "whittle-matern", -1: "var-whittle-matern", 2: "advection-diffus
              7: "var-advection-var-diffusion", 8: "seperable-spatial-temporal"}
 DIFF_CODE = {"iso": 0, "ani": 1, "ha": 2}
 ADV_CODE = {"none": 0, "c": 1, "v": 2, "cov": 3}
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "iterative": 2}
 
 
 def _torch():
@@ -199,6 +199,53 @@ class GPUPlan:
         gbar = gbar.contiguous()
         nat.check(nat.lib().spde_adjoint(self._h, gbar.data_ptr(), g.ctypes.data), self._h, "adjoint")
         return g
+
+    # ---- learned preconditioner and PCG (csrc/pcg.cu)
+    def precond_weights(self, params, with_obs=False, tau=0.0, keep_activations=False):
+        torch = _torch()
+        n = self.grid.n
+        w = torch.empty(n * 27, dtype=torch.float32, device="cuda")
+        act = torch.empty(n * 107, dtype=torch.float32, device="cuda") if keep_activations else None
+        nat.check(nat.lib().spde_precond_weights(self._h, int(with_obs), float(tau), params.data_ptr(), w.data_ptr(),
+                                                 None if act is None else act.data_ptr()), self._h, "precond_weights")
+        return w, act
+
+    def precond_grad(self, params, w, act, z, with_obs=False, tau=0.0):
+        torch = _torch()
+        z = z.to(device="cuda", dtype=torch.float64).contiguous()
+        k = 1 if z.dim() == 1 else z.shape[1]
+        grad = torch.empty_like(params)
+        loss = ctypes.c_double()
+        nat.check(nat.lib().spde_precond_grad(self._h, int(with_obs), float(tau), params.data_ptr(), w.data_ptr(),
+                                              act.data_ptr(), z.data_ptr(), k, ctypes.byref(loss), grad.data_ptr()),
+                  self._h, "precond_grad")
+        return loss.value, grad
+
+    def adam_step(self, params, grad, m, v, t, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        nat.check(nat.lib().spde_adam_step(self._h, params.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(),
+                                           params.numel(), lr, b1, b2, eps, int(t)), self._h, "adam_step")
+
+    def jacobi_smooth(self, z, with_obs=False, tau=0.0, omega=0.6, sweeps=20):
+        """In place: z <- (I - omega D^-1 A)^sweeps z, columns scaled to unit RMS."""
+        nrhs = 1 if z.dim() == 1 else z.shape[1]
+        nat.check(nat.lib().spde_jacobi_smooth(self._h, int(with_obs), float(tau), float(omega), int(sweeps),
+                                               z.data_ptr(), nrhs), self._h, "jacobi_smooth")
+        return z
+
+    def pcg(self, b, with_obs=False, tau=0.0, precond="jacobi", w=None, tol=1e-8, maxit=20000, check=True):
+        """x = A^-1 b by preconditioned CG; precond "none", "jacobi" or "learned" (w)."""
+        torch = _torch()
+        b = b.to(device="cuda", dtype=torch.float64).contiguous()
+        nrhs = 1 if b.dim() == 1 else b.shape[1]
+        x = torch.empty_like(b)
+        kind = {"none": 0, "jacobi": 1, "learned": 2}[precond]
+        it, rel = ctypes.c_int(), ctypes.c_double()
+        rc = nat.lib().spde_pcg(self._h, int(with_obs), float(tau), kind, None if w is None else w.data_ptr(),
+                                b.data_ptr(), x.data_ptr(), nrhs, float(tol), int(maxit), ctypes.byref(it),
+                                ctypes.byref(rel))
+        if rc != 6 or check:
+            nat.check(rc, self._h, "pcg")
+        return x, it.value, rel.value
 
     def loglike(self, canon, y, grad_mode=1, probes=None):
         torch = _torch()

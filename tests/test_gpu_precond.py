@@ -1,0 +1,102 @@
+"""Learned preconditioner and PCG on the GPU: network forward, training loss and
+gradient against the oracle (csrc/pcg.cu vs oracle/precond_oracle.py), PCG
+against the Cholesky solve, and what training gains over Jacobi and plain CG."""
+import numpy as np
+import pytest
+
+from golden_cases import load
+from gpu_cases import gpu_model
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from spdepy_gb300 import build
+    build.build()
+
+
+def _golden_system(precision="fp64", tau=25.0):
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, precision)
+    mod._assemble(g["par"])
+    mod.plan.set_obs(mod.grid.obs_nodes(g["idx"]))
+    return g, mod, tau
+
+
+def test_weights_loss_and_gradient_match_oracle():
+    from oracle import precond_oracle as po
+    from spdepy_gb300.spdes import stencil_to_csr
+    g, mod, tau = _golden_system()
+    plan, grid = mod.plan, mod.grid
+    prm = np.random.default_rng(0).normal(0.0, 0.2, po.NPARAMS).astype(np.float32)
+    p_dev = torch.as_tensor(prm).cuda()
+    w, act = plan.precond_weights(p_dev, True, tau, keep_activations=True)
+    z = np.random.default_rng(1).choice([-1.0, 1.0], size=(grid.n, 3))
+    loss, gr = plan.precond_grad(p_dev, w, act, torch.as_tensor(z), True, tau)
+    A = stencil_to_csr(grid, plan.export_q(True, tau).cpu().numpy())
+    l_ref, g_ref, w_ref = po.loss_grad(prm.astype(np.float64), A, grid.Mx, grid.Ny, grid.T, z)
+    # FP32 network and weights against the FP64 restatement
+    np.testing.assert_allclose(w.view(grid.n, 27).cpu().numpy(), w_ref, rtol=2e-5, atol=2e-6 * np.abs(w_ref).max())
+    assert loss == pytest.approx(l_ref, rel=1e-4)
+    gd = gr.cpu().numpy()
+    assert np.abs(gd - g_ref).max() <= 2e-4 * np.abs(g_ref).max()
+
+
+def test_pcg_matches_cholesky_solve():
+    from spdepy_gb300.precond import LearnedPreconditioner
+    g, mod, tau = _golden_system()
+    plan = mod.plan
+    b = torch.as_tensor(np.random.default_rng(2).normal(size=(mod.grid.n, 2)))
+    plan.factor(True, tau)
+    x_ref, _ = plan.solve(b)
+    x_ref = x_ref.cpu().numpy()
+    lp = LearnedPreconditioner(seed=3)
+    w = lp.weights(plan, True, tau)
+    for kind in ("none", "jacobi", "learned"):
+        x, it, rel = plan.pcg(b, True, tau, kind, w=w, tol=1e-11, maxit=5000)
+        assert rel <= 1e-11 and it > 0
+        assert np.abs(x.cpu().numpy() - x_ref).max() <= 1e-8 * np.abs(x_ref).max()
+
+
+def test_iterative_plan_has_no_factor():
+    import spdepy_gb300._native as nat
+    from spdepy_gb300.workloads import build_model, nonstationary_advection_diffusion
+    w = nonstationary_advection_diffusion(M=20, N=20, T=4)
+    mod = build_model(w, "iterative")
+    mod._assemble(w.par)
+    with pytest.raises(nat.SpdeError):
+        mod.plan.factor(False, 0.0)
+    b = torch.ones(w.grid.n, dtype=torch.float64)
+    x, it, rel = mod.plan.pcg(b, False, 0.0, "jacobi", tol=1e-9)
+    assert rel <= 1e-9
+
+
+def test_training_beats_jacobi_and_plain_cg():
+    """Train on systems drawn from the prior at 24 x 24 x 8, evaluate PCG on
+    held-out parameters at 32 x 32 x 8."""
+    from spdepy_gb300.precond import LearnedPreconditioner, prior_sample, system_maker
+    from spdepy_gb300.workloads import build_model, nonstationary_advection_diffusion
+    wt = nonstationary_advection_diffusion(M=24, N=24, T=8)
+    mt = build_model(wt, "iterative")
+    lp = LearnedPreconditioner(seed=0)
+    hist = lp.train(system_maker(wt, mt), steps=400, probes=4, lr=3e-3, seed=1)
+    assert np.mean(hist[-40:]) < 0.95 * np.mean(hist[:10])
+    we = nonstationary_advection_diffusion(M=32, N=32, T=8, seed=5)
+    me = build_model(we, "iterative")
+    make = system_maker(we, me)
+    rng = np.random.default_rng(123)
+    its = {"none": [], "jacobi": [], "learned": []}
+    for _ in range(3):
+        plan, wo, tau = make(rng)
+        b = torch.as_tensor(rng.normal(size=we.grid.n))
+        wts = lp.weights(plan, wo, tau)
+        for kind in its:
+            _, it, rel = plan.pcg(b, wo, tau, kind, w=wts, tol=1e-8, maxit=20000)
+            assert rel <= 1e-8
+            its[kind].append(it)
+    print("PCG iterations on held-out systems", its)
+    assert sum(its["learned"]) < 0.9 * sum(its["jacobi"]) < sum(its["none"])
