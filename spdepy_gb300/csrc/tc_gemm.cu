@@ -32,15 +32,15 @@ namespace spde {
 namespace {
 
 constexpr int kTM = 128, kTN = 128, kTK = 32;
-constexpr int kConv = 256;                 // loader / converter / epilogue threads (warps 0-7)
-constexpr int kThreads = kConv + 32;       // + one MMA warp
+constexpr int kConv = 256;                 // converter / epilogue threads (warps 0-7)
+constexpr int kLoad = 128;                 // loader threads (warps 8-11)
+constexpr int kThreads = kConv + kLoad + 32;  // + one MMA warp (warp 12)
 constexpr int kPlane = 128 * 32 * 4;       // one 128 x 32 FP32 operand plane (16 KB)
 constexpr int kStages = 4;                 // stage = raw A, raw B, residual B
-constexpr int kAhead = 3;                  // chunks staged ahead of the converters
 constexpr int kStageBytes = 3 * kPlane;
 constexpr int kSmem = kStages * kStageBytes + 1024;
-constexpr int kTmemCols = 256;             // accumulator 0-127, A slots 128-191 and 192-255
-constexpr int kASlot0 = 128, kASlotCols = 64;
+constexpr int kASlot0 = 128, kASlotCols = 64;  // TMEM: accumulator 0-127, A slot s at 128 + 64 s
+constexpr int kTmemCols = 512;             // power of two >= 128 + kStages * 64
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s
 
 __device__ int g_tc_error = 0;
@@ -116,22 +116,26 @@ __device__ __forceinline__ unsigned long long now_ns() {
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int bytes) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, int bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+// the mbarrier receives one arrival when every cp.async this thread issued so far has landed
+__device__ __forceinline__ void cp_async_arrive(uint32_t mbar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Stage one raw 128 x 32 FP32 chunk of an operand into the swizzled tile `dst`
-// (zero outside rows < rows, k < K).  Thread `tid` of the kConv loader threads
-// owns the 16-byte chunks q = tid + i * kConv; row layout with 16-byte aligned
-// rows goes through cp.async, other layouts through registers.
-template <int LAYOUT>
-__device__ __forceinline__ void stage_raw(const float* X, int64_t ld, int rows, int k0, int K, bool vec, uint8_t* dst,
-                                          int tid) {
+// Stage one raw 128 x 32 FP32 chunk of an operand into the swizzled tile at
+// shared address d0 (zero outside rows < rows, k < K) with cp.async: loader
+// thread `tid` of NT copies 16-byte chunks q = tid + i NT when rows are 16-byte
+// aligned (row layout), single elements otherwise (column layout along r).
+template <int LAYOUT, int NT>
+__device__ __forceinline__ void stage_async(const float* X, int64_t ld, int rows, int k0, int K, bool vec, uint32_t d0,
+                                            int tid) {
   if (LAYOUT == kRow && vec) {
-    const uint32_t d0 = smem_u32(dst);
 #pragma unroll
-    for (int it = 0; it < 1024 / kConv; ++it) {
-      const int q = tid + it * kConv;
+    for (int it = 0; it < 1024 / NT; ++it) {
+      const int q = tid + it * NT;
       const int r = q >> 3, c4 = q & 7;
       const int k = k0 + 4 * c4;
       int bytes = 0;
@@ -143,44 +147,20 @@ __device__ __forceinline__ void stage_raw(const float* X, int64_t ld, int rows, 
       cp_async16(d0 + sw_chunk(r, c4), src, bytes);
     }
   } else if (LAYOUT == kRow) {
-#pragma unroll 2
-    for (int it = 0; it < 1024 / kConv; ++it) {
-      const int q = tid + it * kConv;
-      const int r = q >> 3, c4 = q & 7;
-      const int k = k0 + 4 * c4;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (r < rows) {
-        const float* p = X + int64_t(r) * ld + k;
-        if (k < K) v.x = p[0];
-        if (k + 1 < K) v.y = p[1];
-        if (k + 2 < K) v.z = p[2];
-        if (k + 3 < K) v.w = p[3];
-      }
-      *reinterpret_cast<float4*>(dst + sw_chunk(r, c4)) = v;
+#pragma unroll 4
+    for (int it = 0; it < 4096 / NT; ++it) {
+      const int e = tid + it * NT;
+      const int r = e >> 5, kk = e & 31, k = k0 + kk;
+      const bool ok = r < rows && k < K;
+      cp_async4(d0 + sw_chunk(r, kk >> 2) + ((kk & 3) << 2), ok ? X + int64_t(r) * ld + k : X, ok ? 4 : 0);
     }
   } else {
-    // column layout: element (row r, k) at X[k*ld + r]; loads along r
-#pragma unroll 2
-    for (int it = 0; it < 1024 / kConv; ++it) {
-      const int q = tid + it * kConv;
-      const int i4 = q & 31, kk = q >> 5;
-      const int k = k0 + kk;
-      const int r0 = 4 * i4;
-      float v[4] = {0.f, 0.f, 0.f, 0.f};
-      if (k < K) {
-        const float* p = X + int64_t(k) * ld + r0;
-        if (vec && r0 + 3 < rows) {
-          float4 t = *reinterpret_cast<const float4*>(p);
-          v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e)
-            if (r0 + e < rows) v[e] = p[e];
-        }
-      }
-#pragma unroll
-      for (int e = 0; e < 4; ++e)
-        *reinterpret_cast<float*>(dst + sw_chunk(r0 + e, kk >> 2) + ((kk & 3) << 2)) = v[e];
+#pragma unroll 4
+    for (int it = 0; it < 4096 / NT; ++it) {
+      const int e = tid + it * NT;
+      const int r = e & 127, kk = e >> 7, k = k0 + kk;
+      const bool ok = r < rows && k < K;
+      cp_async4(d0 + sw_chunk(r, kk >> 2) + ((kk & 3) << 2), ok ? X + int64_t(k) * ld + r : X, ok ? 4 : 0);
     }
   }
 }
@@ -225,29 +205,18 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
 
-// Barrier among the loader warps only (id 1, kConv threads) that also ANDs a
-// flag, so a failed wait ends the loop for every loader thread together.
-__device__ __forceinline__ bool loader_all(bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n\t.reg .pred pi, po;\n\tsetp.ne.u32 pi, %1, 0;\n\tbar.red.and.pred po, 1, %2, pi;\n\t"
-      "selp.u32 %0, 1, 0, po;\n\t}\n"
-      : "=r"(r)
-      : "r"(uint32_t(v)), "n"(kConv)
-      : "memory");
-  return r != 0;
-}
-
 template <int MODE, int AL, int BL>
 __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __restrict__ tasks, const float* Ab,
                                                               const float* Bb, float* Cb) {
-  // Warps 0-7 stage chunks (cp.async), convert them (A to TMEM, B residual to
-  // shared memory) and run the epilogue; warp 8 issues the MMAs.  Per stage s:
-  // `ready[s]` (kConv arrivals) says chunk t (t % kStages == s) is converted,
-  // `consumed[s]` (tcgen05.commit) says its MMAs are done; `done` follows the
-  // last MMA.
+  // Three roles hand chunk t (stage s = t % kStages) along through mbarriers:
+  //   loaders (warps 8-11): wait consumed[s] (MMAs of chunk t - kStages done),
+  //     issue the cp.async copies of A and B, arrive on full[s] when they land;
+  //   converters (warps 0-7): wait full[s], write A hi/lo into TMEM slot s and
+  //     the B residual plane, arrive on ready[s]; afterwards they run the epilogue;
+  //   MMA issuer (warp 12, one lane): wait ready[s], issue the chunk's 12 MMAs,
+  //     commit to consumed[s]; a final commit arrives on done.
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t ready[kStages], consumed[kStages], done;
+  __shared__ uint64_t full[kStages], ready[kStages], consumed[kStages], done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag, mma_issued;
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -261,6 +230,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full[s])), "r"(kLoad));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&ready[s])), "r"(kConv));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&consumed[s])));
     }
@@ -296,45 +266,20 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
   };
 
   if (warp < kConv / 32) {
-    // ---------------- loaders / converters
-    for (int t = 0; t < kAhead; ++t) {
-      if (t < nk) {
-        uint8_t* st = smem + t * kStageBytes;
-        stage_raw<AL>(A, tk.lda, tk.m, t * kTK, tk.k, avec, st, tid);
-        stage_raw<BL>(B, tk.ldb, tk.n, t * kTK, tk.k, bvec, st + kPlane, tid);
-      }
-      cp_async_commit();
-    }
-    bool ok = true;
+    // ---------------- converters, then the epilogue
     for (int t = 0; t < nk; ++t) {
       const int s = t % kStages;
+      if (!wait(&full[s], uint32_t((t / kStages) & 1), true)) break;
       uint8_t* st = smem + s * kStageBytes;
-      cp_async_wait<kAhead - 1>();  // this thread's copies of chunk t have landed
-      // TMEM slot t & 1 was last read by chunk t - 2
-      if (t >= 2) ok = ok && wait(&consumed[(t - 2) % kStages], uint32_t(((t - 2) / kStages) & 1), true);
-      // all copies of the chunk visible to every converter; failures end the loop together
-      if (!loader_all(ok)) break;
       // warp w reaches TMEM lanes 32 (w % 4) ..; warps 0-3 take k 0-15, warps 4-7 k 16-31
       a_to_tmem(st, tid & 127, tid >> 7,
-                tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(kASlot0 + (t & 1) * kASlotCols));
+                tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(kASlot0 + s * kASlotCols));
       split_b(st + kPlane, st + 2 * kPlane, tid);
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(smem_u32(&ready[s]));
-      const int tn = t + kAhead;
-      if (tn < nk) {
-        // stage tn % kStages last held chunk t - 1, whose MMAs read its B planes
-        if (t >= 1) ok = ok && wait(&consumed[(t - 1) % kStages], uint32_t(((t - 1) / kStages) & 1), true);
-        if (ok) {
-          uint8_t* st2 = smem + (tn % kStages) * kStageBytes;
-          stage_raw<AL>(A, tk.lda, tk.m, tn * kTK, tk.k, avec, st2, tid);
-          stage_raw<BL>(B, tk.ldb, tk.n, tn * kTK, tk.k, bvec, st2 + kPlane, tid);
-        }
-      }
-      cp_async_commit();
     }
-    cp_async_wait<0>();
     const bool fin = nk == 0 || wait(&done, 0u, true);
     if (fin) {
       asm volatile("tcgen05.fence::after_thread_sync;");
@@ -386,6 +331,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
         }
       }
     }
+  } else if (warp < (kConv + kLoad) / 32) {
+    // ---------------- loaders
+    const int ltid = tid - kConv;
+    for (int t = 0; t < nk; ++t) {
+      const int s = t % kStages;
+      // stage s last held chunk t - kStages, read by its MMAs (B) and converters (A)
+      if (t >= kStages && !wait(&consumed[s], uint32_t(((t - kStages) / kStages) & 1), true)) break;
+      const uint32_t d0 = smem_u32(smem + s * kStageBytes);
+      stage_async<AL, kLoad>(A, tk.lda, tk.m, t * kTK, tk.k, avec, d0, ltid);
+      stage_async<BL, kLoad>(B, tk.ldb, tk.n, t * kTK, tk.k, bvec, d0 + kPlane, ltid);
+      cp_async_arrive(smem_u32(&full[s]));
+    }
+    cp_async_wait_all();
   } else if (lane == 0) {
     // ---------------- MMA issuer
     for (int t = 0; t < nk; ++t) {
@@ -393,7 +351,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
       if (!wait(&ready[s], uint32_t((t / kStages) & 1), true)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t rb = smem_u32(smem + s * kStageBytes + kPlane), lb = rb + kPlane;
-      const uint32_t ah = tmem + uint32_t(kASlot0 + (t & 1) * kASlotCols), al = ah + 32;
+      const uint32_t ah = tmem + uint32_t(kASlot0 + s * kASlotCols), al = ah + 32;
 #pragma unroll
       for (int kk = 0; kk < kTK / 8; ++kk) {
         const uint64_t bh = smem_desc(rb + kk * 32), bl = smem_desc(lb + kk * 32);
