@@ -420,10 +420,230 @@ __global__ void __launch_bounds__(256) potrf_kernel(const DiagTask* __restrict__
     }
 }
 
+// ---------------------------------------------- double-float diagonal block
+// The mixed path's diagonal blocks: the same register-blocked right-looking
+// sweep as potrf_kernel, in double-float arithmetic (value = hi + lo, two FP32
+// numbers, about 44 significant bits; Dekker/Knuth error-free transformations
+// with FMA), which runs on the FP32 pipe instead of the narrow FP64 one.  Pivots
+// are converted to FP64 for the log-determinant; L and L^-1 are rounded to FP32
+// for storage (L^-1 from the FP32 L, as in potrf_kernel).
+struct DF {
+  float hi, lo;
+};
+// The _rn intrinsics keep the compiler from contracting the error-free
+// transformations into FMAs.
+__device__ __forceinline__ DF df_renorm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return DF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+// b * c
+__device__ __forceinline__ DF df_mul(DF b, DF c) {
+  const float p = __fmul_rn(b.hi, c.hi);
+  float e = fmaf(b.hi, c.hi, -p);
+  e = fmaf(b.hi, c.lo, e);
+  e = fmaf(b.lo, c.hi, e);
+  return df_renorm(p, e);
+}
+// a - b * c
+__device__ __forceinline__ DF df_fms(DF a, DF b, DF c) {
+  const float p = __fmul_rn(b.hi, c.hi);
+  float e = fmaf(b.hi, c.hi, -p);
+  e = fmaf(b.hi, c.lo, e);
+  e = fmaf(b.lo, c.hi, e);
+  const float s = __fsub_rn(a.hi, p);
+  const float v = __fsub_rn(s, a.hi);
+  float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(-p, v));
+  err = __fadd_rn(err, __fsub_rn(a.lo, e));
+  return df_renorm(s, err);
+}
+// 1 / d: FP32 reciprocal refined by one Newton step with a double-float residual
+__device__ __forceinline__ DF df_rcp(DF d) {
+  const float r = __frcp_rn(d.hi);
+  const DF one_minus = df_fms(DF{1.0f, 0.0f}, d, DF{r, 0.0f});  // 1 - d r
+  return df_renorm(r, __fmul_rn(r, one_minus.hi));
+}
+
+__global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restrict__ tasks, float* __restrict__ L,
+                                                       float* __restrict__ dinv, double* __restrict__ logpiv,
+                                                       int* __restrict__ err) {
+  __shared__ float colh[2][kMaxNbk], coll[2][kMaxNbk];
+  __shared__ float dvh[kMaxNbk], dvl[kMaxNbk];
+  __shared__ double dpiv[kMaxNbk];
+  __shared__ float rsq[kMaxNbk];
+  __shared__ float lsh[kMaxNbk][kMaxNbk + 1];
+  __shared__ float xrow[2][kMaxNbk];
+  __shared__ int bad;
+  const DiagTask tk = tasks[blockIdx.x];
+  const int w = tk.w;
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  float* blk = L + tk.a;
+  DF r[4][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int i = ty + 16 * m, k = tx + 16 * n;
+      r[m][n] = DF{(k <= i && i < w) ? blk[int64_t(i) * tk.lda + k] : 0.0f, 0.0f};
+    }
+  if (tid == 0) bad = 0;
+  // publish column 0 and its pivot reciprocal
+  if (tx == 0) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = ty + 16 * m;
+      if (i < w) { colh[0][i] = r[m][0].hi; coll[0][i] = 0.0f; }
+      if (i == 0) {
+        DF d = r[m][0];
+        if (!(d.hi > 0.0f) || !isfinite(d.hi)) { d = DF{1.0f, 0.0f}; bad = 1; }
+        const DF q = df_rcp(d);
+        dvh[0] = q.hi; dvl[0] = q.lo;
+        dpiv[0] = double(d.hi) + double(d.lo);
+      }
+    }
+  }
+  __syncthreads();
+  for (int j = 0; j < w; ++j) {
+    const float* ch = colh[j & 1];
+    const float* cl = coll[j & 1];
+    const DF dv{dvh[j], dvl[j]};
+    DF ci[4], ck[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = ty + 16 * m;
+      ci[m] = (i > j && i < w) ? df_mul(DF{ch[i], cl[i]}, dv) : DF{0.0f, 0.0f};
+    }
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int k = tx + 16 * n;
+      ck[n] = (k > j && k < w) ? DF{ch[k], cl[k]} : DF{0.0f, 0.0f};
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (16 * m + 15 <= j) continue;
+#pragma unroll
+      for (int n = 0; n <= m; ++n) {
+        if (16 * n + 15 <= j) continue;
+        r[m][n] = df_fms(r[m][n], ci[m], ck[n]);
+      }
+    }
+    // publish column j + 1; the owner of its diagonal also publishes the pivot
+    const int jn = j + 1;
+    if (jn < w && tx == (jn & 15)) {
+      const int n = jn >> 4;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int i = ty + 16 * m;
+        if (i >= jn && i < w) {
+#pragma unroll
+          for (int nn = 0; nn < 4; ++nn)
+            if (nn == n) {
+              colh[jn & 1][i] = r[m][nn].hi;
+              coll[jn & 1][i] = r[m][nn].lo;
+              if (i == jn) {
+                DF d = r[m][nn];
+                if (!(d.hi > 0.0f) || !isfinite(d.hi)) { d = DF{1.0f, 0.0f}; bad = 1; }
+                const DF q = df_rcp(d);
+                dvh[jn] = q.hi; dvl[jn] = q.lo;
+                dpiv[jn] = double(d.hi) + double(d.lo);
+              }
+            }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (tid < w) rsq[tid] = float(1.0 / sqrt(dpiv[tid]));
+  if (tid < 32) {
+    double sum = 0.0;
+    for (int j = tid; j < w; j += 32) sum += 0.5 * log(dpiv[j]);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+    if (tid == 0) {
+      logpiv[blockIdx.x] = sum;
+      if (bad) atomicCAS(err, -1, tk.front);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int i = ty + 16 * m, k = tx + 16 * n;
+      if (i < w && k < w) {
+        const float v = k < i ? (r[m][n].hi + r[m][n].lo) * rsq[k] : (k == i ? 1.0f / rsq[k] : 0.0f);
+        lsh[i][k] = v;
+        blk[int64_t(i) * tk.lda + k] = v;
+      }
+    }
+  float b[4][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) b[m][n] = (ty + 16 * m == tx + 16 * n) ? 1.0f : 0.0f;
+  __syncthreads();
+  if (ty == 0 && tx == 0) {
+    b[0][0] = 1.0f / lsh[0][0];
+    xrow[0][0] = b[0][0];
+  }
+  __syncthreads();
+  for (int j = 0; j < w; ++j) {
+    const float* xr = xrow[j & 1];
+    float li[4], xc[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int i = ty + 16 * m;
+      li[m] = (i > j && i < w) ? lsh[i][j] : 0.0f;
+    }
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int cc = tx + 16 * n;
+      xc[n] = cc <= j ? xr[cc] : 0.0f;
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (16 * m + 15 <= j) continue;
+#pragma unroll
+      for (int n = 0; n <= m; ++n) {
+        if (16 * n > j) continue;
+        b[m][n] = fmaf(-li[m], xc[n], b[m][n]);
+      }
+    }
+    const int jn = j + 1;
+    if (jn < w && ty == (jn & 15)) {
+      const int m = jn >> 4;
+      const float inv = 1.0f / lsh[jn][jn];
+#pragma unroll
+      for (int mm = 0; mm < 4; ++mm) {
+        if (mm != m) continue;
+#pragma unroll
+        for (int n = 0; n < 4; ++n) {
+          const int cc = tx + 16 * n;
+          if (cc <= jn) {
+            b[mm][n] *= inv;
+            xrow[jn & 1][cc] = b[mm][n];
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  float* dvp = dinv + tk.dinv;
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int i = ty + 16 * m, cc = tx + 16 * n;
+      if (i < w && cc < w) dvp[int64_t(i) * kMaxNbk + cc] = cc <= i ? b[m][n] : 0.0f;
+    }
+}
+
 template <typename T>
 void launch_potrf(const DiagTask* tasks, int ntasks, T* L, T* dinv, double* logpiv, int* err, cudaStream_t st) {
   if (ntasks <= 0) return;
-  potrf_kernel<T><<<ntasks, 256, 0, st>>>(tasks, L, dinv, logpiv, err);
+  if constexpr (sizeof(T) == sizeof(float)) {
+    potrf_df_kernel<<<ntasks, 256, 0, st>>>(tasks, L, dinv, logpiv, err);
+  } else {
+    potrf_kernel<T><<<ntasks, 256, 0, st>>>(tasks, L, dinv, logpiv, err);
+  }
 }
 template void launch_potrf<double>(const DiagTask*, int, double*, double*, double*, int*, cudaStream_t);
 template void launch_potrf<float>(const DiagTask*, int, float*, float*, double*, int*, cudaStream_t);
