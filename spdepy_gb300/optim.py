@@ -1,9 +1,12 @@
-"""First-order optimiser driving ``logLike`` (the caller of the GPU hot path).
+"""Optimisers driving ``logLike`` (the caller of the GPU hot path).
 
-Same behaviour as the reference's ``Optimize`` with the Adam step
-(``optim/__init__.py:26-62,152-160``, ``optim/adam.py:3-43``): a fixed number of
-steps, an optional per-step learning-rate schedule, a ``fix`` mask of parameters
-held constant, and Polyak averaging of the last ``pol`` iterates.
+``stepType="adam"`` (default) behaves as the reference's ``Optimize`` with the
+Adam step (``optim/__init__.py:26-62,152-160``, ``optim/adam.py:3-43``): a fixed
+number of steps, an optional per-step learning-rate schedule, a ``fix`` mask of
+parameters held constant, and Polyak averaging of the last ``pol`` iterates.
+``stepType="lbfgs"`` runs limited-memory BFGS (scipy's L-BFGS-B) on the exact
+adjoint gradients, with fixed parameters held by equal bounds; ``max_steps``
+bounds its iterations.
 """
 from __future__ import annotations
 
@@ -43,6 +46,8 @@ class Optimize:
     def fit(self, **kw):
         fun = kw.get("fun", self.fun)
         assert fun is not None
+        if kw.get("stepType", "adam") == "lbfgs":
+            return self._lbfgs(fun, **kw)
         x = np.asarray(kw["x0"], dtype=np.float64).copy()
         lr = kw.get("lr", self.lr)
         steps = kw.get("max_steps") or (len(lr) if hasattr(lr, "__len__") else 100)
@@ -65,4 +70,30 @@ class Optimize:
         res = {"method": "adam", "x": x, "fun": f, "jac": jac}
         if kw.get("end") is not None:
             np.save(kw["end"] + ".npy", x)
+        return res
+
+    def _lbfgs(self, fun, **kw):
+        from scipy.optimize import minimize
+        x0 = np.asarray(kw["x0"], dtype=np.float64).copy()
+        fix = kw.get("fix")
+        bounds = None
+        if fix is not None:
+            mask = np.zeros(x0.size, dtype=bool)
+            mask[fix] = True
+            bounds = [(v, v) if m else (None, None) for v, m in zip(x0, mask)]
+        self.histX, self.histF, self.histJac = [], [], []
+
+        def f(x):
+            val, jac = fun(x)
+            self.histX.append(x.copy())
+            self.histF.append(val)
+            self.histJac.append(jac)
+            return val, jac
+
+        opts = {"maxiter": kw.get("max_steps") or 200, "gtol": kw.get("gtol", 1e-6), "ftol": kw.get("ftol", 1e-12)}
+        r = minimize(f, x0, jac=True, method="L-BFGS-B", bounds=bounds, options=opts)
+        res = {"method": "lbfgs", "x": r.x, "fun": r.fun, "jac": r.jac, "nit": int(r.nit), "nfev": int(r.nfev),
+               "message": str(r.message)}
+        if kw.get("end") is not None:
+            np.save(kw["end"] + ".npy", r.x)
         return res

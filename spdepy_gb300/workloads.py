@@ -79,6 +79,36 @@ def stationary_advection_diffusion(M=100, N=100, T=24, seed=0, obs_per_step=2000
                     np.concatenate(idx), 0.05, mod0_par=mod0)
 
 
+def sensor_track(M, N, T, steps_per_t=2000, seed=3):
+    """Node indices of a 1-cell-wide random walk (4-neighbour moves, reflected at
+    the border) sampled `steps_per_t` times per time step and continued across
+    time steps; revisited cells give repeated observations."""
+    rng = np.random.default_rng(seed)
+    x, y = int(rng.integers(M)), int(rng.integers(N))
+    moves = np.array([(1, 0), (-1, 0), (0, 1), (0, -1)])
+    out = []
+    for t in range(T):
+        for _ in range(steps_per_t):
+            dx, dy = moves[rng.integers(4)]
+            x = x + dx if 0 <= x + dx < M else x - dx
+            y = y + dy if 0 <= y + dy < N else y - dy
+            out.append(t * M * N + y * M + x)
+    return np.asarray(out, dtype=np.int64)
+
+
+def sensor_track_advection_diffusion(M=150, N=150, T=36, seed=3, obs_frac=0.005, steps_per_t=2000):
+    """The non-stationary generator (seed 3) observed at 0.5 % of nodes at random
+    plus a simulated sensor track of 2,000 points per time step, noise sd 0.05."""
+    w = nonstationary_advection_diffusion(M, N, T, seed=seed, obs_frac=obs_frac)
+    track = sensor_track(M, N, T, steps_per_t, seed=seed + 100)
+    w.idx = np.sort(np.concatenate([w.idx, track]))
+    w.noise_sd = 0.05
+    w.par = w.par.copy()
+    w.par[-1] = np.log(1.0 / 0.05 ** 2)
+    w.name = f"nonstationary advection-diffusion {M}x{N}x{T} with sensor track"
+    return w
+
+
 def build_model(w: Workload, precision="mixed"):
     """GPU model object for a workload (observations attached, data simulated)."""
     from .spdes import _CLASSES

@@ -101,3 +101,26 @@ def test_sample_variances_match_selected_inverse():
     rel = emp / var - 1.0
     assert np.abs(rel).max() < 6 * np.sqrt(2.0 / ns)
     assert abs(rel.mean()) < 4 * np.sqrt(2.0 / ns / mod.grid.n) + 0.01
+
+
+def test_lbfgs_fit_reaches_a_stationary_point():
+    """L-BFGS on the exact gradients (the maximum-likelihood fit driver) on the
+    sensor-track generator: lambda, log sigma and log tau free from a perturbed
+    start, everything else held at the truth."""
+    from spdepy_gb300.optim import Optimize
+    from spdepy_gb300.workloads import build_model, sensor_track_advection_diffusion, simulate
+    w = sensor_track_advection_diffusion(M=32, N=30, T=8, steps_per_t=300)
+    mod = build_model(w, "fp64")
+    simulate(mod, w, seed=4)
+    truth = w.par.copy()
+    nb2 = w.grid.Nbs2
+    free = np.array([4 * nb2, 4 * nb2 + 1, truth.size - 1])
+    fix = np.setdiff1d(np.arange(truth.size), free)
+    x0 = truth.copy()
+    x0[free] += np.array([0.4, -0.3, 0.5])
+    res = Optimize(mod.logLike).fit(x0=x0, stepType="lbfgs", max_steps=50, fix=fix)
+    assert np.array_equal(res["x"][fix], truth[fix])
+    assert res["fun"] < mod.logLike(x0, grad=False)
+    assert np.abs(np.asarray(res["jac"])[free]).max() < 1e-5
+    # the estimates move towards the truth
+    assert np.abs(res["x"][free] - truth[free]).max() < np.abs(x0[free] - truth[free]).max()
