@@ -5,23 +5,23 @@
 // 0-127, FP32).  K advances in chunks of 32 FP32 values staged by cp.async into
 // 128-byte-swizzled K-major shared-memory tiles, three chunks ahead of the tensor
 // core (four stages).  Each product runs as 3xTF32: the tensor core reads
-// operands as TF32, so every operand is split into hi = trunc(x) (the 19 high
-// bits) and lo = x - hi rounded to TF32, and one elected thread issues, per
-// 8-wide k step, hi*hi + hi*lo + lo*hi (the lo*lo term, ~2^-21 relative, is
-// dropped), which gives FP32-class products.
+// operands as TF32, so every operand is split (Veltkamp) into an 11-bit hi part
+// and the exact remainder lo, and one elected thread issues, per 8-wide k step,
+// hi*hi + hi*lo + lo*hi (the lo*lo term, under 2^-24 relative, is dropped),
+// which gives FP32-class products.
 //
 // Operand A goes to the tensor core from TMEM: two threads of the eight
 // converter warps own row r of the tile (TMEM lane r), read its 32 raw values of
-// the chunk from shared memory and store hi and lo with tcgen05.st into one of
-// two 64-column TMEM slots (columns 128-255).  Only operand B (raw plane as hi, plus
-// a residual plane) is read by the tensor core from shared memory, which takes
-// the A reads, the A residual writes and half of the tensor core's operand
-// reads off the shared-memory port.
-// Warps 0-7 stage, convert and run the epilogue (two warps per SM sub-partition
-// hide the latency of the conversion); warp 8 issues the MMAs; they hand chunks
-// over through mbarriers (tcgen05.commit arrives when MMAs finish).
+// the chunk from shared memory and store hi and lo with tcgen05.st into the
+// stage's 64-column TMEM slot.  Operand B is read by the tensor core from shared
+// memory: its raw plane rewritten as hi, plus a residual plane.
+// Roles: four loader warps issue cp.async copies whose completion arrives on an
+// mbarrier, eight converter warps split the operands and later run the
+// epilogue, one thread issues the MMAs; stages pass between them through
+// mbarriers (tcgen05.commit arrives when a stage's MMAs finish), so loads,
+// conversions and MMAs of different stages overlap.
 // Every wait is bounded by a wall-clock limit, after which the CTA records an
-// error, frees its tensor memory and returns.
+// error, waits for its issued MMAs, frees its tensor memory and returns.
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -33,8 +33,10 @@ namespace {
 
 constexpr int kTM = 128, kTN = 128, kTK = 32;
 constexpr int kConv = 256;                 // converter / epilogue threads (warps 0-7)
+constexpr int kGroups = 1;                 // converter groups (group g takes chunks t = g mod kGroups)
 constexpr int kLoad = 128;                 // loader threads (warps 8-11)
-constexpr int kThreads = kConv + kLoad + 32;  // + one MMA warp (warp 12)
+constexpr int kThreads = kGroups * kConv + kLoad + 32;  // + one MMA warp (warp 12)
+constexpr int kEpiCols = 128 / (kGroups * kConv / 128);  // accumulator columns per epilogue warp
 constexpr int kPlane = 128 * 32 * 4;       // one 128 x 32 FP32 operand plane (16 KB)
 constexpr int kStages = 4;                 // stage = raw A, raw B, residual B
 constexpr int kStageBytes = 3 * kPlane;
@@ -47,19 +49,6 @@ __device__ int g_tc_error = 0;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ float tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
-// The tensor core reads a 32-bit operand as TF32 by dropping its 13 low mantissa
-// bits; the residual x - trunc(x) is exact in FP32 and is fed rounded to TF32.
-__device__ __forceinline__ float tf32_resid(float x) {
-  const float hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-  return tf32_rna(x - hi);
 }
 
 // byte offset of the 16-byte chunk c4 (k = 4 c4 .. 4 c4 + 3) of row r inside a
@@ -165,16 +154,33 @@ __device__ __forceinline__ void stage_async(const float* X, int64_t ld, int rows
   }
 }
 
-// Residual plane of operand B for one stage: loader thread `tid` converts the
-// 16-byte chunks q = tid + i * kConv.
-__device__ __forceinline__ void split_b(const uint8_t* raw, uint8_t* lo, int tid) {
+// Veltkamp split of an FP32 value for the tensor core: hi = x (2^13 + 1) -
+// (x (2^13 + 1) - x) keeps the 11 leading significant bits (round to nearest),
+// so it is exact in TF32, and lo = x - hi is exact in FP32 with |lo| <= 2^-12 |x|;
+// the tensor core drops lo's bits below TF32, an error under 2^-22 |x|.  Only
+// FP32 adds and multiplies (the _rn forms keep them from being contracted).
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+  const float t = __fmul_rn(x, 8193.0f);
+  hi = __fsub_rn(t, __fsub_rn(t, x));
+  lo = __fsub_rn(x, hi);
+}
+
+// Operand B of one stage: the raw plane is rewritten as its hi part, the lo
+// part goes to the residual plane; converter thread `tid` takes the 16-byte
+// chunks q = tid + i * kConv.
+__device__ __forceinline__ void split_b(uint8_t* raw, uint8_t* lo, int tid) {
 #pragma unroll
   for (int it = 0; it < 1024 / kConv; ++it) {
     const int q = tid + it * kConv;
     const uint32_t off = sw_chunk(q >> 3, q & 7);
     const float4 v = *reinterpret_cast<const float4*>(raw + off);
-    *reinterpret_cast<float4*>(lo + off) =
-        make_float4(tf32_resid(v.x), tf32_resid(v.y), tf32_resid(v.z), tf32_resid(v.w));
+    float4 h, l;
+    split_tf32(v.x, h.x, l.x);
+    split_tf32(v.y, h.y, l.y);
+    split_tf32(v.z, h.z, l.z);
+    split_tf32(v.w, h.w, l.w);
+    *reinterpret_cast<float4*>(raw + off) = h;
+    *reinterpret_cast<float4*>(lo + off) = l;
   }
 }
 
@@ -192,9 +198,10 @@ __device__ __forceinline__ void a_to_tmem(const uint8_t* raw, int row, int h, ui
     const float x[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-      const uint32_t hb = __float_as_uint(x[e]) & 0xFFFFE000u;
-      hi[4 * c + e] = hb;
-      lo[4 * c + e] = __float_as_uint(tf32_rna(x[e] - __uint_as_float(hb)));
+      float h, l;
+      split_tf32(x[e], h, l);
+      hi[4 * c + e] = __float_as_uint(h);
+      lo[4 * c + e] = __float_as_uint(l);
     }
   }
   tmem_st16(taddr + 16 * h, hi);
@@ -212,7 +219,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
   //   loaders (warps 8-11): wait consumed[s] (MMAs of chunk t - kStages done),
   //     issue the cp.async copies of A and B, arrive on full[s] when they land;
   //   converters (warps 0-7): wait full[s], write A hi/lo into TMEM slot s and
-  //     the B residual plane, arrive on ready[s]; afterwards they run the epilogue;
+  //     the B hi/lo planes, arrive on ready[s]; afterwards they run the epilogue;
   //   MMA issuer (warp 12, one lane): wait ready[s], issue the chunk's 12 MMAs,
   //     commit to consumed[s]; a final commit arrives on done.
   extern __shared__ uint8_t smem_raw[];
@@ -265,16 +272,17 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
     return true;
   };
 
-  if (warp < kConv / 32) {
-    // ---------------- converters, then the epilogue
-    for (int t = 0; t < nk; ++t) {
+  if (warp < kGroups * kConv / 32) {
+    // ---------------- converters (two groups on alternate chunks), then the epilogue
+    const int g = tid / kConv, ct = tid - g * kConv;
+    for (int t = g; t < nk; t += kGroups) {
       const int s = t % kStages;
       if (!wait(&full[s], uint32_t((t / kStages) & 1), true)) break;
       uint8_t* st = smem + s * kStageBytes;
-      // warp w reaches TMEM lanes 32 (w % 4) ..; warps 0-3 take k 0-15, warps 4-7 k 16-31
-      a_to_tmem(st, tid & 127, tid >> 7,
+      // warp w reaches TMEM lanes 32 (w % 4) ..; the group's warps 0-3 take k 0-15, warps 4-7 k 16-31
+      a_to_tmem(st, ct & 127, ct >> 7,
                 tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(kASlot0 + s * kASlotCols));
-      split_b(st + kPlane, st + 2 * kPlane, tid);
+      split_b(st + kPlane, st + 2 * kPlane, ct);
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -283,11 +291,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
     const bool fin = nk == 0 || wait(&done, 0u, true);
     if (fin) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      // warp w reads lanes 32 (w % 4) .. and accumulator columns 64 (w / 4) .. + 63
+      // warp w reads lanes 32 (w % 4) .. and accumulator columns kEpiCols (w / 4) ..
       const int row = (warp & 3) * 32 + lane;
 #pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const int col0 = (warp >> 2) * 64 + c * 32;
+      for (int c = 0; c < kEpiCols / 32; ++c) {
+        const int col0 = (warp >> 2) * kEpiCols + c * 32;
         uint32_t r[32];
         const uint32_t ta = tmem + (uint32_t((warp & 3) * 32) << 16) + uint32_t(col0);
         asm volatile(
@@ -331,9 +339,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
         }
       }
     }
-  } else if (warp < (kConv + kLoad) / 32) {
+  } else if (warp < (kGroups * kConv + kLoad) / 32) {
     // ---------------- loaders
-    const int ltid = tid - kConv;
+    const int ltid = tid - kGroups * kConv;
     for (int t = 0; t < nk; ++t) {
       const int s = t % kStages;
       // stage s last held chunk t - kStages, read by its MMAs (B) and converters (A)
