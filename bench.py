@@ -31,8 +31,8 @@ METRIC = "logL+grad evals/s & samples/s, 200x200x24 SPDE: mixed+learned vs FP64 
 
 # DRAM bytes per algorithmic flop of the tensor-core product, from the ncu
 # captures of its two largest launches at 100 x 100 x 24 (an inverse-block
-# product, 4.34e11 flops, and a Schur update, 2.27e11 flops): 2.131e9 bytes.
-TC_DRAM_BYTES_PER_FLOP = 2.131e9 / 6.605e11
+# product, 4.430e11 flops, and a Schur update, 2.270e11 flops): 2.200e9 bytes.
+TC_DRAM_BYTES_PER_FLOP = 2.200e9 / 6.700e11
 
 
 def _tf32_tflops(torch, n=8192, reps=10):
