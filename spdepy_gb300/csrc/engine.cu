@@ -31,6 +31,7 @@ namespace spde {
 
 constexpr int kNbk = 64;  // diagonal block size (kMaxNbk in dense.cu)
 constexpr int kTcMinK = 128;  // shortest K routed to the tensor-core product
+constexpr int kTcMinKUpdate = 64;  // ... for the rank-64 updates inside a factor panel
 enum { KT_NONE = 0, KT_A_UPPER, KT_B_LOWER, KT_BOTH_UPPER };
 constexpr int kPanel = 512;   // panel width of the two-level blocked factorisation
 
@@ -91,8 +92,9 @@ struct Builder {
       o.tc = kPathNarrow;
       return;
     }
+    const int mink = o.site == S_F_UPD ? kTcMinKUpdate : kTcMinK;
     auto mid = std::stable_partition(s.gemm.begin() + beg, s.gemm.begin() + end,
-                                     [](const GemmTask& t) { return t.k >= kTcMinK; });
+                                     [mink](const GemmTask& t) { return t.k >= mink; });
     const int64_t nlong = int64_t(mid - s.gemm.begin()) - beg;
     if (nlong == 0 || beg + nlong == end) {
       o.tc = nlong > 0 ? 1 : 0;
