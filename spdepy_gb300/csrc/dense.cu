@@ -189,6 +189,79 @@ __global__ void __launch_bounds__(256) gemv_kernel(const GemmTask* __restrict__ 
   }
 }
 
+// ------------------------------------------------------ panel solve (FP32)
+// X = A Linv^T for one 64-column diagonal block: tasks with m <= 128 rows,
+// n <= 64 columns and k <= 64, both operands in row layout.  The CTA stages its
+// whole A tile and the block inverse in shared memory once (no K loop), then
+// each thread computes an 8 x 4 block of the output; A may alias C (in-place
+// panel solve): every read happens before the first write.
+constexpr int kPanelLdA = 129, kPanelLdB = 65;
+constexpr int kPanelSmem = (64 * kPanelLdA + 64 * kPanelLdB) * int(sizeof(float));
+
+template <int MODE>
+__global__ void __launch_bounds__(256) panel64_kernel(const GemmTask* __restrict__ tasks, const float* Ab,
+                                                      const float* Bb, float* Cb) {
+  extern __shared__ float psm[];
+  float* As = psm;                     // As[k * kPanelLdA + i] = A(i, k)
+  float* Bs = psm + 64 * kPanelLdA;    // Bs[k * kPanelLdB + j] = B(j, k)
+  const GemmTask tk = tasks[blockIdx.x];
+  const float* A = Ab + tk.a;
+  const float* B = Bb + tk.b;
+  float* C = Cb + tk.c;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < 128 * 64; e += 256) {
+    const int i = e >> 6, k = e & 63;
+    As[k * kPanelLdA + i] = (i < tk.m && k < tk.k) ? A[int64_t(i) * tk.lda + k] : 0.f;
+  }
+  for (int e = tid; e < 64 * 64; e += 256) {
+    const int j = e >> 6, k = e & 63;
+    Bs[k * kPanelLdB + j] = (j < tk.n && k < tk.k) ? B[int64_t(j) * tk.ldb + k] : 0.f;
+  }
+  __syncthreads();
+  const int ty = tid >> 4, tx = tid & 15;  // rows 8 ty .. + 7, columns 4 tx .. + 3
+  float acc[8][4];
+#pragma unroll
+  for (int r = 0; r < 8; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = 0.f;
+  for (int kk = 0; kk < tk.k; ++kk) {
+    float a[8], b[4];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) a[r] = As[kk * kPanelLdA + ty * 8 + r];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) b[c] = Bs[kk * kPanelLdB + tx * 4 + c];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
+  }
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int i = ty * 8 + r;
+    if (i >= tk.m) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int j = tx * 4 + c;
+      if (j >= tk.n) continue;
+      float* dst = C + int64_t(i) * tk.ldc + j;
+      if (MODE == kSub) *dst -= acc[r][c];
+      else if (MODE == kStore) *dst = acc[r][c];
+      else if (MODE == kNegStore) *dst = -acc[r][c];
+      else *dst += acc[r][c];
+    }
+  }
+}
+
+template <int MODE>
+static void panel64_launch(const GemmTask* t, int n, const float* A, const float* B, float* C, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(panel64_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPanelSmem);
+    attr = true;
+  }
+  panel64_kernel<MODE><<<n, 256, kPanelSmem, st>>>(t, A, B, C);
+}
+
 template <typename T, int MODE>
 static void gemv_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, int al, int bl, cudaStream_t st) {
   if (al == kRow && bl == kRow) gemv_kernel<T, MODE, kRow, kRow><<<n, 256, 0, st>>>(t, A, B, C);
@@ -221,6 +294,18 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
     return;
   }
   if constexpr (sizeof(T) == sizeof(float)) {
+    if (path == kPathPanel && alayout == kRow && blayout == kRow) {
+      const float* Af = reinterpret_cast<const float*>(A);
+      const float* Bf = reinterpret_cast<const float*>(B);
+      float* Cf = reinterpret_cast<float*>(C);
+      switch (mode) {
+        case kSub: panel64_launch<kSub>(tasks, ntasks, Af, Bf, Cf, st); break;
+        case kStore: panel64_launch<kStore>(tasks, ntasks, Af, Bf, Cf, st); break;
+        case kNegStore: panel64_launch<kNegStore>(tasks, ntasks, Af, Bf, Cf, st); break;
+        default: panel64_launch<kAdd>(tasks, ntasks, Af, Bf, Cf, st); break;
+      }
+      return;
+    }
     if (path == kPathTensor && tc_gemm_enabled()) {
       launch_gemm_tc(tasks, ntasks, reinterpret_cast<const float*>(A), reinterpret_cast<const float*>(B),
                      reinterpret_cast<float*>(C), mode, alayout, blayout, st);

@@ -92,6 +92,10 @@ struct Builder {
       o.tc = kPathNarrow;
       return;
     }
+    if (o.site == S_F_TRSM) {  // every task: m <= TM, n = k = diagonal block width <= 64
+      o.tc = kPathPanel;
+      return;
+    }
     const int mink = o.site == S_F_UPD ? kTcMinKUpdate : kTcMinK;
     auto mid = std::stable_partition(s.gemm.begin() + beg, s.gemm.begin() + end,
                                      [mink](const GemmTask& t) { return t.k >= mink; });

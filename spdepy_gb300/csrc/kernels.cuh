@@ -41,8 +41,9 @@ struct DevFront {
   int child[2];
 };
 
-// product paths: CUDA-core tiles, tensor-core tiles (FP32 only), narrow (n <= 8 columns)
-enum GemmPath { kPathSimt = 0, kPathTensor = 1, kPathNarrow = 2 };
+// product paths: CUDA-core tiles, tensor-core tiles (FP32 only), narrow (n <= 8
+// columns), panel solve (FP32: m <= 128, n <= 64, k <= 64; CUDA-core tiles otherwise)
+enum GemmPath { kPathSimt = 0, kPathTensor = 1, kPathNarrow = 2, kPathPanel = 3 };
 constexpr int kNarrowMaxN = 8;
 
 template <typename T>
