@@ -208,6 +208,18 @@ int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, i
 int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float* w_dev, const double* b_dev,
              double* x_dev, int nrhs, double tol, int maxit, int* iters, double* relres);
 
+/* Gradient of the objective (spde_loglike's jac, canonical order) for the model
+ * last assembled with log tau = log(tau), on grids too large to factor:
+ * Hutchinson traces (the reference's estimator, advection_diffusion2D.py:200-209)
+ * with the nh1 probe columns probes_dev (n x nh1, +-1, device FP64), every solve
+ * by PCG (precond SPDE_PRECOND_*; w_q_dev / w_qc_dev: G weights for Q and for
+ * Q + tau S^T S) to relative residual tol.  The objective itself needs
+ * log-determinants and is not computed.  *iters receives the PCG iterations
+ * summed over the three solves. */
+int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y_dev, int r, const double* probes_dev, int nh1,
+                          int precond, const float* w_q_dev, const float* w_qc_dev, double tol, int maxit,
+                          double* jac_host, int* iters);
+
 #ifdef __cplusplus
 }
 #endif

@@ -641,6 +641,69 @@ int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, i
   return rc ? SPDE_ERR_CUDA : SPDE_OK;
 }
 
+int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, const double* V, int nh1, int precond,
+                          const float* w_q, const float* w_qc, double tol, int maxit, double* jac, int* iters) {
+  if (!plan || !y || r < 1 || !V || nh1 < 1 || !jac || precond < 0 || precond > 2 ||
+      (precond == 2 && (!w_q || !w_qc)))
+    return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (!p.d_obs_idx || p.nobs < 1) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  cudaStream_t st = p.stream;
+  const int n = p.sym.n, ns = p.sym.nslots, m = p.nobs, ntheta = ntheta_of(p);
+  LoglikeScratch& S = plan->s;
+  const int nblk = 256;
+  API_CUDA(S.part.ensure(nblk));
+  API_CUDA(S.trq.ensure(size_t(n) * nh1));
+  API_CUDA(S.trc.ensure(size_t(n) * nh1));
+  API_CUDA(S.b.ensure(size_t(n) * r));
+  API_CUDA(S.mu.ensure(size_t(n) * r));
+  API_CUDA(S.d.ensure(size_t(m) * r));
+  API_CUDA(S.gbar.ensure(size_t(n) * ns));
+  int it_total = 0, it = 0;
+  double rel = 0.0;
+  auto solve = [&](int with_obs, const float* w, const double* b, double* x, int nrhs) -> int {
+    const int rc = pcg_solve(&p, with_obs, tau, precond, w, b, x, nrhs, tol, maxit, 8, &it, &rel);
+    it_total += it;
+    if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+    if (rc == 6) { p.last_error = "PCG did not reach the tolerance"; return SPDE_ERR_NOT_CONVERGED; }
+    return rc ? SPDE_ERR_CUDA : SPDE_OK;
+  };
+  // conditional mean mu = (Q + tau S^T S)^-1 tau S^T y
+  API_CUDA(cudaMemsetAsync(S.b.p, 0, size_t(n) * r * sizeof(double), st));
+  obs_rhs_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, st>>>(p.d_obs_idx, m, r, tau, y, nullptr, S.b.p);
+  int rc = solve(1, w_qc, S.b.p, S.mu.p, r);
+  if (rc) return rc;
+  // Hutchinson solves Q^-1 V and (Q + tau S^T S)^-1 V
+  if ((rc = solve(0, w_q, V, S.trq.p, nh1))) return rc;
+  if ((rc = solve(1, w_qc, V, S.trc.p, nh1))) return rc;
+  obs_resid_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, st>>>(p.d_obs_idx, m, r, y, S.mu.p, S.d.p);
+  dot_partial_kernel<<<nblk, 256, 0, st>>>(S.d.p, nullptr, int64_t(m) * r, S.part.p);
+  const double rss = host_sum_partials(S.part.p, nblk, st);
+  {
+    const int64_t tot = int64_t(n) * nh1;
+    sub_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(S.trq.p, S.trc.p, tot);
+  }
+  {
+    const int64_t tot = int64_t(n) * ns;
+    gbar_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(p.sym.Mx, p.sym.Ny, p.sym.T, ns, 0.5 * r, nullptr, nullptr,
+                                                        S.trq.p, V, nh1, S.mu.p, r, S.gbar.p);
+  }
+  API_CUDA(S.work.ensure(size_t(adjoint_work_elems(&p))));
+  API_CUDA(S.gradv.ensure(size_t(ntheta)));
+  launch_adjoint(&p, S.gbar.p, S.gradv.p, S.work.p, st);
+  std::vector<double> g(ntheta, 0.0);
+  API_CUDA(cudaMemcpyAsync(g.data(), S.gradv.p, (ntheta - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+  const int centre = p.sym.T == 1 ? 12 : 21;
+  obs_trace_kernel<<<nblk, 256, 0, st>>>(p.d_obs_idx, m, nullptr, ns, centre, S.trc.p, V, nh1, S.part.p);
+  const double tr = host_sum_partials(S.part.p, nblk, st);
+  API_CUDA(cudaGetLastError());
+  g[ntheta - 1] = m * r / 2.0 - 0.5 * r * tau * tr / nh1 - tau / 2 * rss;
+  for (int i = 0; i < ntheta; ++i) jac[i] = -g[i] / (double(m) * r);
+  if (iters) *iters = it_total;
+  return SPDE_OK;
+}
+
 int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float* w, const double* b, double* x,
              int nrhs, double tol, int maxit, int* iters, double* relres) {
   if (!plan || !b || !x || nrhs < 1 || maxit < 1 || !iters || !relres || precond < 0 || precond > 2 ||

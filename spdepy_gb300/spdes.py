@@ -509,6 +509,44 @@ class SpdeModel:
             return f
         return f, self.from_canonical_grad(jc, par)
 
+    def logLikeGradPCG(self, par, precond="jacobi", nh1=64, tol=1e-8, maxit=20000):
+        """Gradient of ``logLike`` for grids too large to factor: the reference's
+        Hutchinson estimator (probes from ``np.random`` as in
+        advection_diffusion2D.py:200) with every solve done by PCG; `precond`
+        is "none", "jacobi" or a ``LearnedPreconditioner``.  Returns (jac,
+        PCG iterations summed over the solves); the objective needs
+        log-determinants and is not computed."""
+        torch = _torch()
+        par = np.asarray(par, dtype=np.float64)
+        if self.data is None:
+            raise RuntimeError("call initFit(data, idx=...) first")
+        self._ensure_model()
+        plan = self.plan
+        plan.set_obs(self.grid.obs_nodes(self.idx))
+        if getattr(self, "_y_pinned", None) is None:
+            self._y_pinned = torch.as_tensor(np.ascontiguousarray(self.data.reshape(-1, self.r))).pin_memory()
+        y = self._y_pinned.to("cuda", non_blocking=True)
+        canon = self.canonical(par)
+        plan.assemble(canon)
+        tau = float(np.exp(canon[-1]))
+        n = self.grid.n
+        v = (2 * np.random.randint(1, 3, n * nh1) - 3).reshape(n, nh1)
+        V = torch.as_tensor(v.astype(np.float64)).cuda()
+        wq = wqc = None
+        if isinstance(precond, str):
+            kind = {"none": 0, "jacobi": 1}[precond]
+        else:
+            kind = 2
+            wq = precond.weights(plan, False, 0.0)
+            wqc = precond.weights(plan, True, tau)
+        jac = np.zeros(canon.size)
+        it = ctypes.c_int()
+        nat.check(nat.lib().spde_loglike_grad_pcg(plan.h, tau, y.data_ptr(), self.r, V.data_ptr(), nh1, kind,
+                                                  None if wq is None else wq.data_ptr(),
+                                                  None if wqc is None else wqc.data_ptr(), float(tol), int(maxit),
+                                                  jac.ctypes.data, ctypes.byref(it)), plan.h, "loglike_grad_pcg")
+        return self.from_canonical_grad(jac, par), it.value
+
     def print(self, par):
         return "| " + ", ".join(f"{k} = {np.mean(np.asarray(par)[s]):.2f}" for k, s in self.layout.sl.items())
 

@@ -100,3 +100,21 @@ def test_training_beats_jacobi_and_plain_cg():
             its[kind].append(it)
     print("PCG iterations on held-out systems", its)
     assert sum(its["learned"]) < 0.9 * sum(its["jacobi"]) < sum(its["none"])
+
+
+def test_hutchinson_gradient_by_pcg_matches_cholesky():
+    """The Hutchinson gradient with every solve by PCG (plain, Jacobi, learned)
+    equals the one with Cholesky solves on the same probes."""
+    from spdepy_gb300.precond import LearnedPreconditioner
+    from spdepy_gb300.workloads import build_model, nonstationary_advection_diffusion, simulate
+    w = nonstationary_advection_diffusion(M=24, N=22, T=6)
+    mod = build_model(w, "fp64")
+    simulate(mod, w)
+    np.random.seed(7)
+    _, j_chol = mod.logLike(w.par, nh1=32, grad=True, grad_mode="hutchinson")
+    lp = LearnedPreconditioner(seed=1)
+    for pc in ("none", "jacobi", lp):
+        np.random.seed(7)
+        j_pcg, its = mod.logLikeGradPCG(w.par, precond=pc, nh1=32, tol=1e-11)
+        assert its > 0
+        np.testing.assert_allclose(j_pcg, j_chol, rtol=1e-7, atol=1e-8 * np.abs(j_chol).max())
