@@ -183,7 +183,8 @@ int spde_conditional_mean(SpdePlan* plan, double tau, const double* y_dev, const
  * Network parameters: SPDE_PRECOND_NPARAMS FP32 values in device memory
  * (layout W1[32][42], b1[32], W2[32][32], b2[32], W3[27][32], b3[27]). */
 int spde_precond_nparams(void);
-/* G weights (n x 27, FP32, device) for the assembled model; act_dev (optional,
+/* G weights (27 x n, offset-major: weight of offset o = (dt+1) 9 + (dy+1) 3 +
+ * (dx+1) at node p in w_dev[o n + p]; FP32, device) for the assembled model; act_dev (optional,
  * n x 107 FP32) keeps the activations a gradient step needs. */
 int spde_precond_weights(SpdePlan* plan, int with_obs, double tau, const float* params_dev, float* w_dev,
                          float* act_dev);

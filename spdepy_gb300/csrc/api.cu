@@ -620,6 +620,7 @@ int spde_precond_grad(SpdePlan* plan, int with_obs, double tau, const float* par
   if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   const int rc = pc_grad(&p, with_obs, tau, params, w, act, z, k, loss, grad);
   if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+  if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
   return rc ? SPDE_ERR_CUDA : SPDE_OK;
 }
 
@@ -638,6 +639,7 @@ int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, i
   if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   const int rc = jacobi_smooth(&p, with_obs, tau, omega, sweeps, z, nrhs);
   if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+  if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
   return rc ? SPDE_ERR_CUDA : SPDE_OK;
 }
 
@@ -666,6 +668,7 @@ int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, co
     const int rc = pcg_solve(&p, with_obs, tau, precond, w, b, x, nrhs, tol, maxit, 8, &it, &rel);
     it_total += it;
     if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+    if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
     if (rc == 6) { p.last_error = "PCG did not reach the tolerance"; return SPDE_ERR_NOT_CONVERGED; }
     return rc ? SPDE_ERR_CUDA : SPDE_OK;
   };
@@ -714,6 +717,7 @@ int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float*
   if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   const int rc = pcg_solve(&p, with_obs, tau, precond, w, b, x, nrhs, tol, maxit, 8, iters, relres);
   if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
+  if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
   if (rc == 6) { p.last_error = "PCG did not reach the tolerance"; return SPDE_ERR_NOT_CONVERGED; }
   return rc ? SPDE_ERR_CUDA : SPDE_OK;
 }

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const int* 
     int dx, dy, dt;
     off27(o, &dx, &dy, &dt);
     const bool in = inside(q, x + dx, y + dy, t + dt);
-    w[p * kOff + o] = in ? ((o == 13 ? 1.f : 0.f) + a) * s : 0.f;
+    w[int64_t(o) * n + p] = in ? ((o == 13 ? 1.f : 0.f) + a) * s : 0.f;
   }
   if (act) {
     float* ap = act + p * kAct;
@@ -114,43 +114,47 @@ __global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const int* 
   }
 }
 
-// out = G x (transpose = 0) or G^T x (transpose = 1); x, out n x nrhs row-major.
+// out = G x (transpose = 0) or G^T x (transpose = 1); x, out n x nrhs row-major;
+// weights offset-major (w[o n + p]), so every offset's read is coalesced.  The
+// 27 offsets are unrolled (compile-time displacements, loads issued together);
+// node indices fit in 32 bits (checked by the caller).
+template <int TRANS>
 __global__ void pc_apply_kernel(QStencil q, const float* __restrict__ w, const double* __restrict__ x,
-                                double* __restrict__ out, int nrhs, int transpose) {
-  const int64_t n = int64_t(q.Ns) * q.T;
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+                                double* __restrict__ out, int nrhs) {
+  const int n = q.Ns * q.T;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
-  const int64_t p = e / nrhs;
-  const int r = int(e - p * nrhs);
-  const int t = int(p / q.Ns), c = int(p - int64_t(t) * q.Ns);
+  const int p = nrhs == 1 ? e : e / nrhs;
+  const int r = e - p * nrhs;
+  const int t = p / q.Ns, c = p - t * q.Ns;
   const int y = c / q.Mx, xx = c - y * q.Mx;
-  double acc = 0.0;
+  const int sy = q.Mx, st = q.Ns;
+  // FP32 arithmetic: a preconditioner only has to be a fixed SPD operator, and
+  // FP64 is a narrow pipe on this part
+  float acc = 0.f;
+#pragma unroll
   for (int o = 0; o < kOff; ++o) {
-    int dx, dy, dt;
-    off27(o, &dx, &dy, &dt);
-    if (!transpose) {
-      if (!inside(q, xx + dx, y + dy, t + dt)) continue;
-      const int64_t nb = p + (int64_t(dt) * q.Ny + dy) * q.Mx + dx;
-      acc = fma(double(w[p * kOff + o]), x[nb * nrhs + r], acc);
-    } else {
-      if (!inside(q, xx - dx, y - dy, t - dt)) continue;
-      const int64_t nb = p - (int64_t(dt) * q.Ny + dy) * q.Mx - dx;
-      acc = fma(double(w[nb * kOff + o]), x[nb * nrhs + r], acc);
-    }
+    const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+    const int sgn = TRANS ? -1 : 1;
+    const int x2 = xx + sgn * dx, y2 = y + sgn * dy, t2 = t + sgn * dt;
+    if (x2 < 0 || x2 >= q.Mx || y2 < 0 || y2 >= q.Ny || t2 < 0 || t2 >= q.T) continue;
+    const int nb = p + sgn * (dt * st + dy * sy + dx);
+    const float wv = TRANS ? w[int64_t(o) * n + nb] : w[int64_t(o) * n + p];
+    acc = fmaf(wv, float(x[int64_t(nb) * nrhs + r]), acc);
   }
-  out[e] = acc;
+  out[e] = double(acc);
 }
 
 // Jacobi: out = x / A_pp
 __global__ void pc_jacobi_kernel(QStencil q, const int* __restrict__ obs, double tau, const double* __restrict__ x,
                                  double* __restrict__ out, int nrhs) {
-  const int64_t n = int64_t(q.Ns) * q.T;
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int n = q.Ns * q.T;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
-  const int64_t p = e / nrhs;
-  const int t = int(p / q.Ns), c = int(p - int64_t(t) * q.Ns);
+  const int p = nrhs == 1 ? e : e / nrhs;
+  const int t = p / q.Ns, c = p - t * q.Ns;
   const double d = qval(q, c, t, 0, 0, 0) + (obs ? tau * obs[p] : 0.0);
-  out[e] = x[e] / d;
+  out[e] = double(__fdividef(float(x[e]), float(d)));  // FP32: see pc_apply_kernel
 }
 
 // e = z - v (in place into v)
@@ -302,7 +306,7 @@ __global__ void pcg_xr_kernel(double* __restrict__ x, double* __restrict__ r, co
                               const double* __restrict__ pap, const int* __restrict__ done, int64_t n, int nrhs) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
-  const int c = int(e % nrhs);
+  const int c = nrhs == 1 ? 0 : int(e % nrhs);
   if (done[c]) return;
   const double alpha = pap[c] > 0.0 ? rz[c] / pap[c] : 0.0;
   x[e] = fma(alpha, p[e], x[e]);
@@ -313,7 +317,7 @@ __global__ void pcg_p_kernel(double* __restrict__ p, const double* __restrict__ 
                              const double* __restrict__ rzo, const int* __restrict__ done, int64_t n, int nrhs) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
-  const int c = int(e % nrhs);
+  const int c = nrhs == 1 ? 0 : int(e % nrhs);
   if (done[c]) return;
   const double beta = rzo[c] != 0.0 ? rzn[c] / rzo[c] : 0.0;
   p[e] = fma(beta, p[e], z[e]);
@@ -373,8 +377,8 @@ void apply_precond(Plan* p, int kind, const float* w, const int* obs, double tau
   } else if (kind == 1) {
     pc_jacobi_kernel<<<nblk(len), 256, 0, p->stream>>>(q, obs, tau, r, z, nrhs);
   } else {
-    pc_apply_kernel<<<nblk(len), 256, 0, p->stream>>>(q, w, r, tmp, nrhs, 0);
-    pc_apply_kernel<<<nblk(len), 256, 0, p->stream>>>(q, w, tmp, z, nrhs, 1);
+    pc_apply_kernel<0><<<nblk(len), 256, 0, p->stream>>>(q, w, r, tmp, nrhs);
+    pc_apply_kernel<1><<<nblk(len), 256, 0, p->stream>>>(q, w, tmp, z, nrhs);
   }
 }
 
@@ -395,6 +399,7 @@ int pc_weights(Plan* p, int with_obs, double tau, const float* prm, float* w, fl
 int pc_grad(Plan* p, int with_obs, double tau, const float* prm, const float* w, const float* act, const double* z,
             int k, double* loss, float* grad) {
   const int64_t n = p->sym.n, len = n * k;
+  if (len >= (int64_t(1) << 31)) return 1;  // the stencil kernels index entries in 32 bits
   const int nbw = int((n + kBwNodes - 1) / kBwNodes);
   // y, u, e, g1, g2 (n x k doubles each) + partial sums + per-node dout and block partials (as floats)
   const size_t dbl = size_t(5 * len) + size_t(kDotBlocks) * k + 8;
@@ -408,11 +413,11 @@ int pc_grad(Plan* p, int with_obs, double tau, const float* prm, const float* w,
   const QStencil q = p->qstencil();
   const int* obs = with_obs ? p->d_obs_cnt : nullptr;
   cudaStream_t st = p->stream;
-  pc_apply_kernel<<<nblk(len), 256, 0, st>>>(q, w, z, y, k, 1);           // y = G^T z
+  pc_apply_kernel<1><<<nblk(len), 256, 0, st>>>(q, w, z, y, k);           // y = G^T z
   launch_spmv(q, obs, tau, y, u, k, st);                                   // u = A y
-  pc_apply_kernel<<<nblk(len), 256, 0, st>>>(q, w, u, e, k, 0);           // v = G u
+  pc_apply_kernel<0><<<nblk(len), 256, 0, st>>>(q, w, u, e, k);           // v = G u
   pc_sub_kernel<<<nblk(len), 256, 0, st>>>(z, e, len);                     // e = z - v
-  pc_apply_kernel<<<nblk(len), 256, 0, st>>>(q, w, e, g1, k, 1);          // G^T e
+  pc_apply_kernel<1><<<nblk(len), 256, 0, st>>>(q, w, e, g1, k);          // G^T e
   launch_spmv(q, obs, tau, g1, g2, k, st);                                 // g = A G^T e
   // loss = ||e||^2 / (n k): one column of length n k
   pc_dot_partial_kernel<<<kDotBlocks, 256, 0, st>>>(e, e, len, 1, part);
@@ -460,6 +465,7 @@ int jacobi_smooth(Plan* p, int with_obs, double tau, double omega, int sweeps, d
 int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const double* b, double* x, int nrhs,
               double tol, int maxit, int check_every, int* iters, double* relres) {
   const int64_t n = p->sym.n, len = n * nrhs;
+  if (len >= (int64_t(1) << 31)) return 1;  // the stencil kernels index entries in 32 bits
   const size_t need = size_t(5 * len) + size_t(kDotBlocks) * nrhs + size_t(8 * nrhs) + size_t(nrhs);
   double* base = scratch(p, need);
   if (!base) return 4;

@@ -40,7 +40,7 @@ def test_weights_loss_and_gradient_match_oracle():
     A = stencil_to_csr(grid, plan.export_q(True, tau).cpu().numpy())
     l_ref, g_ref, w_ref = po.loss_grad(prm.astype(np.float64), A, grid.Mx, grid.Ny, grid.T, z)
     # FP32 network and weights against the FP64 restatement
-    np.testing.assert_allclose(w.view(grid.n, 27).cpu().numpy(), w_ref, rtol=2e-5, atol=2e-6 * np.abs(w_ref).max())
+    np.testing.assert_allclose(w.view(27, grid.n).T.cpu().numpy(), w_ref, rtol=2e-5, atol=2e-6 * np.abs(w_ref).max())
     assert loss == pytest.approx(l_ref, rel=1e-4)
     gd = gr.cpu().numpy()
     assert np.abs(gd - g_ref).max() <= 2e-4 * np.abs(g_ref).max()
