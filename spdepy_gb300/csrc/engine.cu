@@ -92,7 +92,10 @@ struct Builder {
       o.tc = kPathNarrow;
       return;
     }
-    if (o.site == S_F_TRSM) {  // every task: m <= TM, n = k = diagonal block width <= 64
+    // panel solves, and look-ahead updates of one block column: m <= TM, n <= 64, k <= 64
+    bool panel = (o.site == S_F_TRSM || o.site == S_F_UPD) && end > beg;
+    for (int64_t i = beg; i < end && panel; ++i) panel = s.gemm[i].n <= kNbk && s.gemm[i].k <= kNbk;
+    if (panel) {
       o.tc = kPathPanel;
       return;
     }
@@ -233,8 +236,12 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         b.gemm_tiles(a, x.ld, x.ld, x.d_off + int64_t(kb) * kNbk * kNbk, kNbk, kNbk, a, x.ld, rows, w, w);
       }
       b.end();
-      // rank-64 update of the remaining columns of this 512-column panel
+      // Updates inside this 512-column panel, by pairs of diagonal blocks (the
+      // panel holds an even number of them): after the first block of a pair only
+      // the next block column is updated (rank 64, look-ahead), after the second
+      // the rest of the panel at once (rank 128).
       const int pstart = (kb * kNbk) / kPanel * kPanel, pend = pstart + kPanel;
+      const bool first_of_pair = ((kb * kNbk - pstart) / kNbk) % 2 == 0;
       Op& ou = b.begin(OP_GEMM);
       ou.site = S_F_UPD; ou.mode = kSub; ou.al = kRow; ou.bl = kRow;
       ou.abuf = B_L; ou.bbuf = B_L; ou.cbuf = B_L;
@@ -243,10 +250,13 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         if (x.ns <= kb * kNbk) continue;
         int w = std::min(kNbk, x.ns - kb * kNbk);
         int c0 = kb * kNbk + w, c1 = std::min(x.ns, pend);
+        if (first_of_pair) c1 = std::min(c1, c0 + kNbk);
         if (c0 >= c1) continue;
+        const int k0 = first_of_pair ? kb * kNbk : (kb - 1) * kNbk;  // first column of the update's K range
         int rows = x.ns + x.nb - c0, cols = c1 - c0;
-        int64_t a = x.p_off + int64_t(c0) * x.ld + kb * kNbk;
-        b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.p_off + int64_t(c0) * x.ld + c0, x.ld, rows, cols, w, true);
+        int64_t a = x.p_off + int64_t(c0) * x.ld + k0;
+        b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.p_off + int64_t(c0) * x.ld + c0, x.ld, rows, cols,
+                     kb * kNbk + w - k0, true);
       }
       b.end();
       // at the end of a panel: one update of all later separator columns with K = panel width
