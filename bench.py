@@ -431,6 +431,8 @@ def main():
                      "traffic_source": "ncu dram bytes per flop of two captured launches (100x100x24), "
                                        "scaled by this run's flops per launch",
                      "launches_per_step": float(pct[9] / args.steps),
+                     "note": "launch durations measured while the Q and Q + tau S^T S pipelines run concurrently "
+                             "on two streams (per-class times below are summed over both)",
                      "share_of_step": tc_ms / (ms / args.steps),
                      "tf32_cublas_tflops": tf32,
                      "frac_of_3xtf32": achieved / (tf32 / 3.0) if tf32 else None},

@@ -113,6 +113,12 @@ int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* c
 /* The same timing split by call site of the tiled product (18 entries: factor
  * panel solve / panel update / Schur update, solve steps, inverse steps). */
 int spde_plan_read_sites(SpdePlan* plan, double* ms, double* flops, int64_t* tiles, int reset);
+/* Concurrency of spde_loglike (no reference counterpart): with 2 pipelines (the
+ * default) Q + tau S^T S is factored, solved and inverted on a second set of
+ * arenas with its own stream and host thread while Q runs on the plan's own, so
+ * the two factorisations' latency-bound top levels overlap; it doubles the
+ * factor and inverse memory.  1 runs them one after the other on one set. */
+int spde_plan_set_pipelines(SpdePlan* plan, int pipelines);
 /* Symbolic analysis without a GPU (host only): statistics and the ordering. */
 int spde_symbolic_info(int Mx, int Ny, int T, int leaf_max, SpdePlanInfo* info);
 int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int32_t* front_ns, int32_t* front_nb,

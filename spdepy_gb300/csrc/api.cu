@@ -5,7 +5,9 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <memory>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "../../include/spde_gb300.h"
@@ -163,6 +165,12 @@ struct LoglikeScratch {
 struct SpdePlan {
   Plan p;
   LoglikeScratch s;
+  // Second pipeline of spde_loglike: Q + tau S^T S is factored, solved and
+  // inverted on its own arenas and stream while Q runs on the plan's own, so the
+  // latency-bound top levels of the two overlap.  It shares the assembled model
+  // and the observations of `p` (read only) and is built on first use.
+  std::unique_ptr<Plan> twin;
+  int pipelines = 2;
 };
 
 extern "C" {
@@ -219,6 +227,65 @@ int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int
   return SPDE_OK;
 }
 
+// Frees what plan_build and the solve / iterative paths allocated for a plan
+// (not its model or observation arrays).
+static void release_numeric(Plan& p) {
+  void* ptrs[] = {p.d_fronts, p.d_perm, p.d_iperm, p.d_front_of, p.d_blist, p.d_rmap, p.d_amap, p.d_L, p.d_dinv,
+                  p.d_pool[0], p.d_pool[1], p.d_logpiv, p.d_err, p.d_scalar, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0],
+                  p.d_G[1], p.d_r, p.d_x64, p.d_b64, p.d_part, p.d_sx, p.d_pc};
+  for (void* q : ptrs) cudaFree(q);
+  for (cudaEvent_t e : p.ev_pool) cudaEventDestroy(e);
+  p.ev_pool.clear();
+  p.sched_factor.release();
+  p.sched_selinv.release();
+  for (auto& kv : p.sched_fwd) kv.second->release();
+  for (auto& kv : p.sched_bwd) kv.second->release();
+}
+
+static void destroy_twin(SpdePlan* plan) {
+  if (!plan->twin) return;
+  Plan& t = *plan->twin;
+  cudaStreamSynchronize(t.stream);
+  release_numeric(t);
+  if (t.stream) cudaStreamDestroy(t.stream);
+  plan->twin.reset();
+}
+
+static int ensure_twin(SpdePlan* plan) {
+  if (plan->twin) return SPDE_OK;
+  Plan& p = plan->p;
+  std::unique_ptr<Plan> t(new (std::nothrow) Plan());
+  if (!t) return SPDE_ERR_NO_MEMORY;
+  t->precision = p.precision;
+  t->sym = p.sym;
+  if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    p.last_error = "could not create the second pipeline's stream";
+    return SPDE_ERR_CUDA;
+  }
+  const int rc = plan_build(t.get());
+  if (rc) {
+    p.last_error = "second pipeline: " + t->last_error;
+    release_numeric(*t);
+    cudaStreamDestroy(t->stream);
+    return rc == 4 ? SPDE_ERR_NO_MEMORY : SPDE_ERR_CUDA;
+  }
+  plan->twin = std::move(t);
+  return SPDE_OK;
+}
+
+// The twin reads the plan's assembled model and observations (same device arrays).
+static void share_model(const Plan& p, Plan& t) {
+  t.model = p.model;
+  t.model_set = p.model_set;
+  t.d_Q0 = p.d_Q0; t.d_QA = p.d_QA; t.d_QO = p.d_QO; t.d_cQs = p.d_cQs;
+  t.cfac = p.cfac;
+  t.assembled = p.assembled;
+  t.d_obs_cnt = p.d_obs_cnt;
+  t.d_obs_idx = p.d_obs_idx;
+  t.nobs = p.nobs;
+  t.profile = p.profile;
+}
+
 static int no_factor(SpdePlan* plan) {
   plan->p.last_error = "this plan was created for iterative solves only (no factorisation)";
   return SPDE_ERR_STATE;
@@ -256,6 +323,7 @@ int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePla
 
 int spde_plan_destroy(SpdePlan* plan) {
   if (!plan) return SPDE_OK;
+  destroy_twin(plan);
   Plan& p = plan->p;
   cudaStreamSynchronize(p.stream);
   void* ptrs[] = {p.d_fronts, p.d_perm, p.d_iperm, p.d_front_of, p.d_blist, p.d_rmap, p.d_amap, p.d_L, p.d_dinv,
@@ -289,7 +357,7 @@ int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info) {
   info->precision = p.precision;
   info->bytes_factor = double(p.sym.l_size) * p.esize();
   info->bytes_work = double(p.pool_elems[0] + p.pool_elems[1]) * p.esize();
-  info->launches = p.launches_total;
+  info->launches = p.launches_total + (plan->twin ? plan->twin->launches_total : 0);
   return SPDE_OK;
 }
 
@@ -299,31 +367,49 @@ int spde_plan_set_profiling(SpdePlan* plan, int enable) {
   if (!plan) return SPDE_ERR_ARG;
   prof_collect(&plan->p);
   plan->p.profile = enable != 0;
+  if (plan->twin) {
+    prof_collect(plan->twin.get());
+    plan->twin->profile = enable != 0;
+  }
   return SPDE_OK;
 }
 
 int spde_plan_read_sites(SpdePlan* plan, double* ms, double* flops, int64_t* tiles, int reset) {
   if (!plan) return SPDE_ERR_ARG;
-  Plan& p = plan->p;
-  prof_collect(&p);
+  Plan* ps[2] = {&plan->p, plan->twin.get()};
+  for (Plan* q : ps)
+    if (q) prof_collect(q);
   for (int k = 0; k < S_COUNT; ++k) {
-    if (ms) ms[k] = p.site_ms[k];
-    if (flops) flops[k] = p.site_flops[k];
-    if (tiles) tiles[k] = p.site_tiles[k];
-    if (reset) { p.site_ms[k] = 0; p.site_flops[k] = 0; p.site_tiles[k] = 0; }
+    double a = 0.0, b = 0.0;
+    int64_t c = 0;
+    for (Plan* q : ps) {
+      if (!q) continue;
+      a += q->site_ms[k]; b += q->site_flops[k]; c += q->site_tiles[k];
+      if (reset) { q->site_ms[k] = 0; q->site_flops[k] = 0; q->site_tiles[k] = 0; }
+    }
+    if (ms) ms[k] = a;
+    if (flops) flops[k] = b;
+    if (tiles) tiles[k] = c;
   }
   return SPDE_OK;
 }
 
 int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* count, int reset) {
   if (!plan) return SPDE_ERR_ARG;
-  Plan& p = plan->p;
-  prof_collect(&p);
+  Plan* ps[2] = {&plan->p, plan->twin.get()};
+  for (Plan* q : ps)
+    if (q) prof_collect(q);
   for (int k = 0; k < kProfClasses; ++k) {
-    if (ms) ms[k] = p.prof_ms[k];
-    if (flops) flops[k] = p.prof_flops[k];
-    if (count) count[k] = p.prof_count[k];
-    if (reset) { p.prof_ms[k] = 0; p.prof_flops[k] = 0; p.prof_count[k] = 0; }
+    double a = 0.0, b = 0.0;
+    int64_t c = 0;
+    for (Plan* q : ps) {
+      if (!q) continue;
+      a += q->prof_ms[k]; b += q->prof_flops[k]; c += q->prof_count[k];
+      if (reset) { q->prof_ms[k] = 0; q->prof_flops[k] = 0; q->prof_count[k] = 0; }
+    }
+    if (ms) ms[k] = a;
+    if (flops) flops[k] = b;
+    if (count) count[k] = c;
   }
   return SPDE_OK;
 }
@@ -545,23 +631,55 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   if (hutch) { API_CUDA(S.trq.ensure(size_t(n) * nh1)); API_CUDA(S.trc.ensure(size_t(n) * nh1)); }
   const int iters = p.precision == 0 ? 1 : 10;
   const double tol = kRefineTol;
-  // Q: log-determinant, then its inverse on the pattern (or Hutchinson solves)
-  double ldq = 0.0, ldqc = 0.0, res = 0.0;
-  if ((rc = plan_factor(&p, 0, 0.0))) return rc;
-  ldq = p.logdet;
-  if (exact && (rc = plan_selinv(&p, S.zq.p))) return rc;
-  if (hutch && (rc = plan_solve(&p, V, S.trq.p, nh1, iters, tol, &res))) return rc;
-  // Q_c = Q + tau S^T S
-  if ((rc = plan_factor(&p, 1, tau))) return rc;
-  ldqc = p.logdet;
   API_CUDA(S.b.ensure(size_t(n) * r));
   API_CUDA(S.mu.ensure(size_t(n) * r));
   API_CUDA(S.qmu.ensure(size_t(n) * r));
   API_CUDA(S.d.ensure(size_t(m) * r));
-  API_CUDA(cudaMemsetAsync(S.b.p, 0, size_t(n) * r * sizeof(double), st));
-  obs_rhs_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, st>>>(p.d_obs_idx, m, r, tau, y, nullptr, S.b.p);
-  if ((rc = plan_solve(&p, S.b.p, S.mu.p, r, iters, tol, &res))) return rc;
-  if (hutch && (rc = plan_solve(&p, V, S.trc.p, nh1, iters, tol, &res))) return rc;
+  // Q_c = Q + tau S^T S on the second pipeline when there is one (its own
+  // arenas, stream and host thread), else after Q on this plan
+  Plan* qc = &p;
+  if (plan->pipelines > 1) {
+    if ((rc = ensure_twin(plan))) return rc;
+    qc = plan->twin.get();
+    share_model(p, *qc);
+    cudaEvent_t ready;
+    API_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    API_CUDA(cudaEventRecord(ready, st));  // assembly done
+    API_CUDA(cudaStreamWaitEvent(qc->stream, ready, 0));
+    cudaEventDestroy(ready);
+  }
+  double ldq = 0.0, ldqc = 0.0, res = 0.0, res_c = 0.0;
+  int rc_c = 0;
+  auto run_qc = [&]() {
+    if ((rc_c = plan_factor(qc, 1, tau))) return;
+    ldqc = qc->logdet;
+    cudaMemsetAsync(S.b.p, 0, size_t(n) * r * sizeof(double), qc->stream);
+    obs_rhs_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, qc->stream>>>(p.d_obs_idx, m, r, tau, y, nullptr,
+                                                                               S.b.p);
+    if ((rc_c = plan_solve(qc, S.b.p, S.mu.p, r, iters, tol, &res_c))) return;
+    if (hutch && (rc_c = plan_solve(qc, V, S.trc.p, nh1, iters, tol, &res_c))) return;
+    if (exact && (rc_c = plan_selinv(qc, S.zqc.p))) return;
+  };
+  std::thread worker;
+  if (qc != &p) {
+    try {
+      worker = std::thread(run_qc);
+    } catch (...) {
+      qc = &p;  // no thread available: both on this plan, one after the other
+    }
+  }
+  // Q: log-determinant, then its inverse on the pattern (or Hutchinson solves)
+  rc = plan_factor(&p, 0, 0.0);
+  if (!rc) ldq = p.logdet;
+  if (!rc && exact) rc = plan_selinv(&p, S.zq.p);
+  if (!rc && hutch) rc = plan_solve(&p, V, S.trq.p, nh1, iters, tol, &res);
+  if (qc != &p) worker.join();
+  else if (!rc) run_qc();
+  if (rc) return rc;
+  if (rc_c) {
+    if (qc != &p) p.last_error = qc->last_error;
+    return rc_c;
+  }
   // quadratic terms
   launch_spmv(p.qstencil(), nullptr, 0.0, S.mu.p, S.qmu.p, r, st);
   dot_partial_kernel<<<nblk, 256, 0, st>>>(S.mu.p, S.qmu.p, int64_t(n) * r, S.part.p);
@@ -573,7 +691,6 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   const double like = 0.5 * ldq * r + m * r * std::log(tau) / 2 - 0.5 * ldqc * r - 0.5 * muqmu - tau / 2 * rss;
   *f_out = -like / (double(m) * r);
   if (!grad_mode) return SPDE_OK;
-  if (exact && (rc = plan_selinv(&p, S.zqc.p))) return rc;
   API_CUDA(S.gbar.ensure(size_t(n) * ns));
   if (hutch) {
     int64_t tot = int64_t(n) * nh1;
@@ -598,6 +715,13 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   const double trace_term = exact ? tr : tr / nh1;
   g[ntheta - 1] = m * r / 2.0 - 0.5 * r * tau * trace_term - tau / 2 * rss;
   for (int i = 0; i < ntheta; ++i) jac[i] = -g[i] / (double(m) * r);
+  return SPDE_OK;
+}
+
+int spde_plan_set_pipelines(SpdePlan* plan, int pipelines) {
+  if (!plan || pipelines < 1 || pipelines > 2) return SPDE_ERR_ARG;
+  plan->pipelines = pipelines;
+  if (pipelines == 1) destroy_twin(plan);
   return SPDE_OK;
 }
 

@@ -955,7 +955,7 @@ static int factor_t(Plan* p, int with_obs, double tau) {
   CUDA_TRY(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   CUDA_TRY(cudaGetLastError());
-  if (tc_gemm_take_error()) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
+  if (tc_gemm_take_error(p->stream)) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
   if (err >= 0) {
     char buf[128];
     std::snprintf(buf, sizeof(buf), "matrix is not positive definite (front %d)", err);
@@ -1066,7 +1066,7 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
   }
   CUDA_TRY(cudaGetLastError());
   if (p->profile) prof_collect(p);
-  if (tc_gemm_take_error()) { p->last_error = "tensor-core product timed out"; return 2; }
+  if (tc_gemm_take_error(p->stream)) { p->last_error = "tensor-core product timed out"; return 2; }
   return 0;
 }
 
@@ -1112,7 +1112,7 @@ static int selinv_t(Plan* p, double* zq) {
   p->launches_total += 1;
   CUDA_TRY(cudaStreamSynchronize(st));
   CUDA_TRY(cudaGetLastError());
-  if (tc_gemm_take_error()) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
+  if (tc_gemm_take_error(p->stream)) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
   if (p->profile) prof_collect(p);
   p->factored = 0;  // the factor's panels now hold intermediate products
   return 0;

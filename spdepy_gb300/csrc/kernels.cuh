@@ -54,7 +54,7 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
 // bounded-wait error flag of that kernel.
 void launch_gemm_tc(const GemmTask* tasks, int ntasks, const float* A, const float* B, float* C, int mode, int al,
                     int bl, cudaStream_t st);
-int tc_gemm_take_error();
+int tc_gemm_take_error(cudaStream_t st);
 bool tc_gemm_enabled();
 
 template <typename T>

@@ -415,10 +415,16 @@ void launch_gemm_tc(const GemmTask* tasks, int ntasks, const float* A, const flo
   }
 }
 
-int tc_gemm_take_error() {
-  int h = 0, z = 0;
-  cudaMemcpyFromSymbol(&h, g_tc_error, sizeof(int));
-  if (h) cudaMemcpyToSymbol(g_tc_error, &z, sizeof(int));
+int tc_gemm_take_error(cudaStream_t st) {
+  // stream-ordered, so a second pipeline on another stream is not serialised
+  int h = 0;
+  static const int z = 0;
+  cudaMemcpyFromSymbolAsync(&h, g_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  if (h) {
+    cudaMemcpyToSymbolAsync(g_tc_error, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+    cudaStreamSynchronize(st);
+  }
   return h;
 }
 
