@@ -61,3 +61,18 @@ def test_selinv_solve_sample_mixed_vs_fp64(pair):
     assert np.abs(xm - x64).max() <= 1e-4 * np.abs(x64).max()
     mask = z64 != 0
     assert np.abs(zm - z64)[mask].max() <= 1e-4 * np.abs(z64).max()
+
+
+def test_one_and_two_pipelines_agree(pair):
+    """spde_loglike with the Q and Q + tau S^T S pipelines on two streams gives the
+    same numbers as with both on one (the kernels are deterministic)."""
+    from spdepy_gb300 import _native as nat
+    w, m64, mmx = pair
+    f2, g2 = mmx.logLike(w.par, grad=True)
+    nat.check(nat.lib().spde_plan_set_pipelines(mmx.plan.h, 1), mmx.plan.h)
+    try:
+        f1, g1 = mmx.logLike(w.par, grad=True)
+    finally:
+        nat.check(nat.lib().spde_plan_set_pipelines(mmx.plan.h, 2), mmx.plan.h)
+    assert f1 == f2
+    np.testing.assert_array_equal(g1, g2)
