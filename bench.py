@@ -183,7 +183,15 @@ def learned_pcg_leg(train_steps=5000):
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         out[kind] = {"iterations": it, "relres": rel, "ms": round(dt * 1e3, 2), "ms_per_iteration": round(dt * 1e3 / max(it, 1), 3)}
-    del me, mt
+    # 64 posterior draws without a factorisation: x = mu + A^-1 (B^T e1 + sqrt(tau) S^T e2), Q = B^T B
+    me.initFit(b[idx] / tau, idx=idx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xs, its = me.samplePosteriorPCG(n=64, precond=lp, seed=3, tol=1e-6)
+    torch.cuda.synchronize()
+    out["posterior_samples"] = {"draws": 64, "iterations": its, "ms": round((time.perf_counter() - t0) * 1e3, 1),
+                                "precond": "learned", "tol": 1e-6}
+    del me, mt, xs
     return out
 
 

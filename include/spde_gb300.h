@@ -202,6 +202,12 @@ int spde_precond_grad(SpdePlan* plan, int with_obs, double tau, const float* par
 /* One Adam update of n parameters on the plan's stream (step t >= 1). */
 int spde_adam_step(SpdePlan* plan, float* params_dev, const float* grad_dev, float* m_dev, float* v_dev, int n,
                    double lr, double b1, double b2, double eps, int t);
+/* Square root of the prior precision, Q = B^T B (no reference counterpart; the
+ * time-block structure of spdes/advection_diffusion2D.py:101-116 written as a
+ * sum of squares): y = B x (transpose 0) or B^T x (transpose 1), n x nrhs
+ * row-major, device FP64.  B^T eps with eps ~ N(0, I) has covariance Q, which
+ * gives posterior draws by one PCG solve (Model.sample without a factor). */
+int spde_qsqrt(SpdePlan* plan, int transpose, const double* x_dev, double* y_dev, int nrhs);
 /* z <- (I - omega D^-1 A)^sweeps z, then every column scaled to unit RMS
  * (z_dev n x nrhs, FP64): the error a damped-Jacobi sweep leaves after
  * `sweeps` steps from z, i.e. the smooth residual directions CG has to work on;

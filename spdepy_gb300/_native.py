@@ -78,6 +78,7 @@ SIGNATURES = {
     "spde_precond_weights": (_I, [_P, _I, _D, _P, _P, _P]),
     "spde_precond_grad": (_I, [_P, _I, _D, _P, _P, _P, _P, _I, ctypes.POINTER(_D), _P]),
     "spde_adam_step": (_I, [_P, _P, _P, _P, _P, _I, _D, _D, _D, _D, _I]),
+    "spde_qsqrt": (_I, [_P, _I, _P, _P, _I]),
     "spde_jacobi_smooth": (_I, [_P, _I, _D, _D, _I, _P, _I]),
     "spde_loglike_grad_pcg": (_I, [_P, _D, _P, _I, _P, _I, _I, _P, _P, _D, _I, _P, ctypes.POINTER(_I)]),
     "spde_pcg": (_I, [_P, _I, _D, _I, _P, _P, _P, _I, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),

@@ -756,6 +756,15 @@ int spde_adam_step(SpdePlan* plan, float* params, const float* grad, float* m, f
              : SPDE_OK;
 }
 
+int spde_qsqrt(SpdePlan* plan, int transpose, const double* x, double* y, int nrhs) {
+  if (!plan || !x || !y || nrhs < 1) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  const int rc = qsqrt_apply(&p, transpose, x, y, nrhs);
+  if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
+  return rc ? SPDE_ERR_CUDA : SPDE_OK;
+}
+
 int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, int sweeps, double* z, int nrhs) {
   if (!plan || !z || nrhs < 1 || sweeps < 0) return SPDE_ERR_ARG;
   Plan& p = plan->p;

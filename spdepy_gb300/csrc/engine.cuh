@@ -162,6 +162,7 @@ int pc_grad(Plan* p, int with_obs, double tau, const float* prm, const float* w,
             int k, double* loss, float* grad);
 int pc_adam(const float* g, float* prm, float* m, float* v, int n, float lr, float b1, float b2, float eps, int t,
             cudaStream_t st);
+int qsqrt_apply(Plan* p, int transpose, const double* x, double* y, int nrhs);
 int jacobi_smooth(Plan* p, int with_obs, double tau, double omega, int sweeps, double* z, int nrhs);
 int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const double* b, double* x, int nrhs,
               double tol, int maxit, int check_every, int* iters, double* relres);

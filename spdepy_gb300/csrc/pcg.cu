@@ -291,6 +291,27 @@ __global__ void pc_dot_partial_kernel(const double* __restrict__ a, const double
     __syncthreads();
   }
 }
+// The same for many columns: lane = column within a 32-column chunk
+// (blockIdx.y), warps stride over the rows, so each row segment is read
+// contiguously; part[r * gridDim.x + block] as in pc_dot_partial_kernel.
+__global__ void pc_dot_wide_kernel(const double* __restrict__ a, const double* __restrict__ b, int64_t n, int nrhs,
+                                   double* __restrict__ part) {
+  __shared__ double red[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = blockIdx.y * 32 + lane;
+  double acc = 0.0;
+  if (r < nrhs)
+    for (int64_t i = int64_t(blockIdx.x) * 8 + warp; i < n; i += int64_t(gridDim.x) * 8)
+      acc += a[i * nrhs + r] * b[i * nrhs + r];
+  red[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0 && r < nrhs) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += red[w][lane];
+    part[int64_t(r) * gridDim.x + blockIdx.x] = s;
+  }
+}
+
 __global__ void pc_dot_final_kernel(const double* __restrict__ part, int nblocks, int nrhs, double* __restrict__ out) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrhs) return;
@@ -383,11 +404,77 @@ void apply_precond(Plan* p, int kind, const float* w, const int* obs, double tau
 }
 
 void col_dots(Plan* p, const double* a, const double* b, int nrhs, double* part, double* out) {
-  pc_dot_partial_kernel<<<kDotBlocks, 256, 0, p->stream>>>(a, b, p->sym.n, nrhs, part);
+  if (nrhs == 1) {
+    pc_dot_partial_kernel<<<kDotBlocks, 256, 0, p->stream>>>(a, b, p->sym.n, 1, part);
+  } else {
+    const dim3 grid(kDotBlocks, (nrhs + 31) / 32);
+    pc_dot_wide_kernel<<<grid, 256, 0, p->stream>>>(a, b, p->sym.n, nrhs, part);
+  }
   pc_dot_final_kernel<<<nblk(nrhs, 64), 64, 0, p->stream>>>(part, kDotBlocks, nrhs, out);
 }
 
+// Square root of Q: Q = B^T B with B (n x n) stacking, for the initial field,
+// V^-1/2 A0 (rows (c, 0)) and, for each step t -> t + 1, sqrt(c qs_c) (A x_(t+1)
+// / V - x_t) (rows (c, t + 1)); for a spatial model (T = 1) B = V^-1/2 A.  A and
+// A0 are the 9-point implicit-Euler and initial-field operators (A_geo[c 9 + p]
+// = A[c, c + off_p], off_p = (p % 3 - 1, p / 3 - 1)), qs = V kappa^2, c =
+// 1 / (dt sigma) (spdes/advection_diffusion2D.py:101-116 written as a sum of squares).
+// out = B x (TRANS = 0) or B^T x (TRANS = 1), n x nrhs row-major.
+template <int TRANS>
+__global__ void qsqrt_kernel(int Mx, int Ny, int T, const double* __restrict__ Ag, const double* __restrict__ A0g,
+                             const double* __restrict__ qs, double V, double cfac, const double* __restrict__ x,
+                             double* __restrict__ out, int nrhs) {
+  const int Ns = Mx * Ny, n = Ns * T;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int k = nrhs == 1 ? e : e / nrhs;
+  const int r = e - k * nrhs;
+  const int t = k / Ns, c = k - t * Ns;
+  const int cy = c / Mx, cx = c - cy * Mx;
+  const double rv = 1.0 / sqrt(V);
+  double acc = 0.0;
+  if (!TRANS) {
+    // row (c, t)
+    const double* Ar = (T > 1 && t == 0 ? A0g : Ag) + int64_t(c) * 9;
+    double sum = 0.0;
+#pragma unroll
+    for (int p = 0; p < 9; ++p) {
+      const int x2 = cx + p % 3 - 1, y2 = cy + p / 3 - 1;
+      if (x2 < 0 || x2 >= Mx || y2 < 0 || y2 >= Ny) continue;
+      sum = fma(Ar[p], x[int64_t(t * Ns + y2 * Mx + x2) * nrhs + r], sum);
+    }
+    if (T == 1 || t == 0) acc = rv * sum;
+    else acc = sqrt(cfac * qs[c]) * (sum / V - x[int64_t((t - 1) * Ns + c) * nrhs + r]);
+  } else {
+    // column (c, t): rows (c', t) with c = c' + off_p, and the -1 of row (c, t + 1)
+#pragma unroll
+    for (int p = 0; p < 9; ++p) {
+      const int x2 = cx - (p % 3 - 1), y2 = cy - (p / 3 - 1);
+      if (x2 < 0 || x2 >= Mx || y2 < 0 || y2 >= Ny) continue;
+      const int c2 = y2 * Mx + x2;
+      const double xe = x[int64_t(t * Ns + c2) * nrhs + r];
+      if (T == 1 || t == 0) acc = fma(rv * (T > 1 ? A0g : Ag)[int64_t(c2) * 9 + p], xe, acc);
+      else acc = fma(sqrt(cfac * qs[c2]) * Ag[int64_t(c2) * 9 + p] / V, xe, acc);
+    }
+    if (T > 1 && t + 1 < T) acc -= sqrt(cfac * qs[c]) * x[int64_t((t + 1) * Ns + c) * nrhs + r];
+  }
+  out[e] = acc;
+}
+
 }  // namespace
+
+int qsqrt_apply(Plan* p, int transpose, const double* x, double* y, int nrhs) {
+  const int64_t len = int64_t(p->sym.n) * nrhs;
+  if (len >= (int64_t(1) << 31)) return 1;
+  const int Mx = p->sym.Mx, Ny = p->sym.Ny, T = p->sym.T;
+  if (transpose)
+    qsqrt_kernel<1><<<nblk(len), 256, 0, p->stream>>>(Mx, Ny, T, p->d_Ageo, p->d_A0geo, p->d_qs, p->model.V, p->cfac,
+                                                      x, y, nrhs);
+  else
+    qsqrt_kernel<0><<<nblk(len), 256, 0, p->stream>>>(Mx, Ny, T, p->d_Ageo, p->d_A0geo, p->d_qs, p->model.V, p->cfac,
+                                                      x, y, nrhs);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
 
 int pc_weights(Plan* p, int with_obs, double tau, const float* prm, float* w, float* act) {
   const int64_t n = p->sym.n;

@@ -225,6 +225,16 @@ class GPUPlan:
         nat.check(nat.lib().spde_adam_step(self._h, params.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(),
                                            params.numel(), lr, b1, b2, eps, int(t)), self._h, "adam_step")
 
+    def qsqrt(self, x, transpose=False):
+        """B x (or B^T x) with Q = B^T B for the assembled model (FP64)."""
+        torch = _torch()
+        x = x.to(device="cuda", dtype=torch.float64).contiguous()
+        y = torch.empty_like(x)
+        nrhs = 1 if x.dim() == 1 else x.shape[1]
+        nat.check(nat.lib().spde_qsqrt(self._h, int(bool(transpose)), x.data_ptr(), y.data_ptr(), nrhs), self._h,
+                  "qsqrt")
+        return y
+
     def jacobi_smooth(self, z, with_obs=False, tau=0.0, omega=0.6, sweeps=20):
         """In place: z <- (I - omega D^-1 A)^sweeps z, columns scaled to unit RMS."""
         nrhs = 1 if z.dim() == 1 else z.shape[1]
@@ -546,6 +556,39 @@ class SpdeModel:
                                                   None if wqc is None else wqc.data_ptr(), float(tol), int(maxit),
                                                   jac.ctypes.data, ctypes.byref(it)), plan.h, "loglike_grad_pcg")
         return self.from_canonical_grad(jac, par), it.value
+
+    def samplePosteriorPCG(self, n=1, precond="jacobi", seed=None, tol=1e-8, maxit=20000):
+        """Posterior draws without a factorisation: x = mu + A^-1 (B^T e1 +
+        sqrt(tau) S^T e2) with A = Q + tau S^T S, Q = B^T B, e1, e2 ~ N(0, I)
+        (covariance A^-1 (Q + tau S^T S) A^-1 = A^-1), every solve by PCG.
+        Returns (n_nodes x n draws on the device, PCG iterations)."""
+        torch = _torch()
+        if self.data is None:
+            raise RuntimeError("call initFit(data, idx=...) first")
+        self._ensure_model()
+        plan = self.plan
+        nodes = self.grid.obs_nodes(self.idx)
+        plan.set_obs(nodes)
+        canon = self.canonical(self.par)
+        plan.assemble(canon)
+        tau = float(np.exp(canon[-1]))
+        rng = np.random.default_rng(seed)
+        nn = self.grid.n
+        e1 = torch.as_tensor(rng.normal(size=(nn, n))).cuda()
+        e2 = torch.as_tensor(rng.normal(size=(nodes.size, n))).cuda()
+        rhs = torch.zeros(nn, n + 1, dtype=torch.float64, device="cuda")
+        rhs[:, :n] = plan.qsqrt(e1, transpose=True)
+        ix = torch.as_tensor(nodes).cuda()
+        rhs[:, :n].index_add_(0, ix, np.sqrt(tau) * e2)
+        y = torch.as_tensor(np.asarray(self.data, dtype=np.float64).reshape(-1, self.r)[:, 0]).cuda()
+        rhs[:, n].index_add_(0, ix, tau * y)
+        w = None
+        kind = precond
+        if not isinstance(precond, str):
+            kind = "learned"
+            w = precond.weights(plan, True, tau)
+        x, its, _ = plan.pcg(rhs.contiguous(), True, tau, kind, w=w, tol=tol, maxit=maxit)
+        return x[:, :n] + x[:, n:n + 1], its
 
     def print(self, par):
         return "| " + ", ".join(f"{k} = {np.mean(np.asarray(par)[s]):.2f}" for k, s in self.layout.sl.items())

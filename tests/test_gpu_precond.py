@@ -118,3 +118,46 @@ def test_hutchinson_gradient_by_pcg_matches_cholesky():
         j_pcg, its = mod.logLikeGradPCG(w.par, precond=pc, nh1=32, tol=1e-11)
         assert its > 0
         np.testing.assert_allclose(j_pcg, j_chol, rtol=1e-7, atol=1e-8 * np.abs(j_chol).max())
+
+
+@pytest.mark.parametrize("name", ["advdiff_ani_bc3", "covadv_vardiff_bc1", "wm_ani_bc1"])
+def test_square_root_of_q(name):
+    """B^T B x == Q x for the square root used by the factor-free samplers."""
+    g = load(name)
+    mod = gpu_model(g, "fp64")
+    mod._assemble(g["par"])
+    plan = mod.plan
+    x = torch.as_tensor(np.random.default_rng(3).normal(size=(mod.grid.n, 3)))
+    qx = plan.spmv(x).cpu().numpy()
+    btbx = plan.qsqrt(plan.qsqrt(x), transpose=True).cpu().numpy()
+    np.testing.assert_allclose(btbx, qx, rtol=0, atol=1e-12 * np.abs(qx).max())
+    # the transpose is the adjoint
+    z = torch.as_tensor(np.random.default_rng(4).normal(size=(mod.grid.n, 3))).cuda()
+    lhs = (plan.qsqrt(x) * z).sum().item()
+    rhs = (x.cuda() * plan.qsqrt(z, transpose=True)).sum().item()
+    assert lhs == pytest.approx(rhs, rel=1e-12)
+
+
+def test_posterior_draws_by_pcg_match_cholesky():
+    """Factor-free posterior draws (B^T e1 + sqrt(tau) S^T e2 through PCG) equal
+    the Cholesky solve of the same perturbations."""
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, "fp64")
+    x_pcg, its = mod.samplePosteriorPCG(n=4, precond="jacobi", seed=9, tol=1e-12)
+    assert its > 0
+    plan = mod.plan
+    tau = float(np.exp(mod.canonical(mod.par)[-1]))
+    rng = np.random.default_rng(9)
+    nn = mod.grid.n
+    e1 = torch.as_tensor(rng.normal(size=(nn, 4))).cuda()
+    nodes = mod.grid.obs_nodes(mod.idx)
+    e2 = torch.as_tensor(rng.normal(size=(nodes.size, 4))).cuda()
+    rhs = plan.qsqrt(e1, transpose=True)
+    rhs.index_add_(0, torch.as_tensor(nodes).cuda(), np.sqrt(tau) * e2)
+    b = torch.zeros(nn, dtype=torch.float64, device="cuda")
+    b.index_add_(0, torch.as_tensor(nodes).cuda(), tau * torch.as_tensor(np.asarray(g["y"], float)).cuda())
+    plan.factor(True, tau)
+    mu, _ = plan.solve(b)
+    xs, _ = plan.solve(rhs)
+    ref = (xs + mu[:, None]).cpu().numpy()
+    np.testing.assert_allclose(x_pcg.cpu().numpy(), ref, rtol=0, atol=1e-9 * np.abs(ref).max())
