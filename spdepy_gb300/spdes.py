@@ -100,6 +100,8 @@ class GPUPlan:
         self.nslots = 25 if grid.T == 1 else 43
         self.layout = None
         self._obs = None
+        self._akey = None   # parameters of the assembled model
+        self._fkey = None   # (parameters, with_obs, tau) of the factor the plan holds
 
     @property
     def h(self):
@@ -148,6 +150,8 @@ class GPUPlan:
     def assemble(self, canon):
         canon = np.ascontiguousarray(canon, dtype=np.float64)
         nat.check(nat.lib().spde_assemble(self._h, canon.ctypes.data, canon.size), self._h, "assemble")
+        self._akey = canon.tobytes()
+        self._fkey = None
 
     def export_q(self, with_obs=False, tau=0.0):
         torch = _torch()
@@ -157,7 +161,9 @@ class GPUPlan:
 
     def factor(self, with_obs=False, tau=0.0):
         ld = ctypes.c_double()
+        self._fkey = None
         nat.check(nat.lib().spde_factor(self._h, int(with_obs), float(tau), ctypes.byref(ld)), self._h, "factor")
+        self._fkey = (self._akey, bool(with_obs), float(tau))
         return ld.value
 
     def solve(self, b, refine=None, tol=1e-12):
@@ -182,6 +188,7 @@ class GPUPlan:
     def selinv(self):
         torch = _torch()
         z = torch.empty(self.grid.n * self.nslots, dtype=torch.float64, device="cuda")
+        self._fkey = None  # the selected inversion overwrites the factor
         nat.check(nat.lib().spde_selinv(self._h, z.data_ptr()), self._h, "selinv")
         return z.view(self.grid.n, self.nslots)
 
@@ -270,6 +277,7 @@ class GPUPlan:
             probes = probes.to(device="cuda", dtype=torch.float64).contiguous()
             nh1 = probes.shape[1]
             pp = probes.data_ptr()
+        self._fkey = None  # the evaluation factors (and inverts) internally
         nat.check(nat.lib().spde_loglike(self._h, canon.ctypes.data, canon.size, y.data_ptr(), r, grad_mode, pp, nh1,
                                          ctypes.byref(f), jac.ctypes.data), self._h, "loglike")
         return f.value, jac
@@ -318,19 +326,61 @@ def stencil_to_csr(grid, qv):
 
 
 class Factor:
-    """Factor-like handle (the reference's ``cholesky(Q)`` result, B2 interface)."""
+    """Factor handle: the reference's ``cholesky(Q)`` result (B2 interface:
+    ``logdet``, ``solve_A``, ``solve_Lt``, ``apply_Pt``).  The GPU plan holds
+    one factorisation at a time; a handle refactors on use when the plan has
+    moved on (another factorisation, a selected inversion, a log-likelihood)."""
 
-    def __init__(self, spde, with_obs, tau, logdet):
+    def __init__(self, spde, with_obs, tau, logdet, par=None):
         self.spde, self.with_obs, self.tau, self._logdet = spde, with_obs, tau, logdet
+        self.par = None if par is None else np.asarray(par, dtype=np.float64).copy()
+        self._key = spde.plan._fkey
 
     def logdet(self):
         return self._logdet
 
+    def _ensure(self):
+        plan = self.spde.plan
+        if plan._fkey is None or plan._fkey != self._key:
+            if self.par is None:
+                raise RuntimeError("the plan no longer holds this factorisation")
+            self.spde._assemble(self.par)
+            plan.factor(self.with_obs, self.tau)
+            self._key = plan._fkey
+        return plan
+
     def solve_A(self, b):
         torch = _torch()
+        plan = self._ensure()
         bt = torch.as_tensor(np.asarray(b, dtype=np.float64)) if isinstance(b, np.ndarray) else b
-        x, _ = self.spde.plan.solve(bt)
+        x, _ = plan.solve(bt)
         return x.cpu().numpy() if isinstance(b, np.ndarray) else x
+
+    def solve_Lt(self, b, use_LDLt_decomposition=False):
+        """First half of the reference's sampler ``apply_Pt(solve_Lt(z))``
+        (model.py:79-84).  The product L^-T and the permutation run as one GPU
+        call, so this returns a deferred value that ``apply_Pt`` completes:
+        apply_Pt(solve_Lt(z)) = P L^-T P^T z, a draw from N(0, Q^-1) for
+        z ~ N(0, I) (the factor's ordering is not CHOLMOD's, so the draws
+        differ from the reference's while having the same distribution)."""
+        if use_LDLt_decomposition:
+            raise NotImplementedError("the GPU factor is LL^T")
+        return _LtSolve(self, b)
+
+    def apply_Pt(self, v):
+        if not isinstance(v, _LtSolve):
+            raise NotImplementedError("apply_Pt completes solve_Lt(z); pass its result")
+        torch = _torch()
+        plan = self._ensure()
+        z = v.z
+        zt = torch.as_tensor(np.asarray(z, dtype=np.float64)) if isinstance(z, np.ndarray) else z
+        x = plan.sample(zt)
+        return x.cpu().numpy() if isinstance(z, np.ndarray) else x
+
+
+class _LtSolve:
+    def __init__(self, factor, z):
+        self.factor, self.z = factor, z
 
 
 class SpdeModel:
@@ -462,7 +512,7 @@ class SpdeModel:
         par = np.asarray(par, dtype=np.float64)
         self._assemble(par)
         ld = self.plan.factor(False, 0.0)
-        return PrecisionQ(self, par), Factor(self, False, 0.0, ld), None
+        return PrecisionQ(self, par), Factor(self, False, 0.0, ld, par), None
 
     def setQ(self, par=None, S=None):
         if par is None:

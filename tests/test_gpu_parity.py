@@ -158,3 +158,26 @@ def test_facade_update_golden():
     m.setModel()
     m.update(g["y"], g["idx"])
     assert np.allclose(m.mu, g["mu"], rtol=1e-10, atol=1e-12)
+
+
+def test_factor_handle_survives_other_factorisations():
+    """makeQ's factor handle (the reference's cholesky(Q)) keeps solving with Q
+    after the plan has factored Q + tau S^T S and run a log-likelihood, and
+    apply_Pt(solve_Lt(z)) draws from N(0, Q^-1) as the reference's sampler does."""
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, "fp64")
+    Q, fac, _ = mod.makeQ(g["par"])
+    b = np.random.default_rng(1).normal(size=mod.grid.n)
+    x0 = fac.solve_A(b)
+    mod.logLike(g["par"], grad=True)          # refactors and inverts internally
+    mod.plan.factor(True, 25.0)
+    x1 = fac.solve_A(b)
+    np.testing.assert_allclose(x1, x0, rtol=1e-12, atol=1e-12 * np.abs(x0).max())
+    Qs = Q.to_scipy()
+    np.testing.assert_allclose(Qs @ x1, b, rtol=0, atol=1e-9 * np.abs(b).max())
+    z = np.random.default_rng(2).normal(size=(mod.grid.n, 2000))
+    xs = fac.apply_Pt(fac.solve_Lt(z))
+    # E[x x^T] = Q^-1: check the quadratic form of the empirical covariance
+    v = np.random.default_rng(3).normal(size=mod.grid.n)
+    emp = np.mean((v @ xs) ** 2)
+    assert emp == pytest.approx(v @ fac.solve_A(v), rel=0.15)
