@@ -250,6 +250,46 @@ def lbfgs_fit_leg(max_steps=60):
             "grad_inf_fit": float(np.abs(np.asarray(res["jac"])[free]).max()), "hutchinson_pcg_gradient": hutch}
 
 
+def config2_leg():
+    """Stationary advection-diffusion, 100 x 100 x 24 (240,000 nodes), 2,000
+    observations per step, sigma = 0.05, bc 1: the mixed plan (FP32 factor with
+    3xTF32 products, FP64 pivots and refinement) against the FP64 plan for logL,
+    the exact gradient and 256 samples drawn from the same z."""
+    import torch
+    from spdepy_gb300.workloads import build_model, simulate, stationary_advection_diffusion
+    w = stationary_advection_diffusion()
+    out = {"workload": w.name + f" ({w.grid.n} nodes, {w.idx.size} observations)"}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        mod = build_model(w, prec)
+        if prec == "fp64":
+            simulate(mod, w)
+        else:
+            mod.initFit(w.y, idx=w.idx)
+        mod.logLike(w.par, grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f, jac = mod.logLike(w.par, grad=True)
+        torch.cuda.synchronize()
+        t_eval = time.perf_counter() - t0
+        mod._assemble(w.par)
+        mod.plan.factor(False, 0.0)
+        z = torch.as_tensor(np.random.default_rng(7).normal(size=(w.grid.n, 256))).cuda()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x = mod.plan.sample(z)
+        torch.cuda.synchronize()
+        res[prec] = (f, jac, x.cpu().numpy(), t_eval, time.perf_counter() - t0)
+        del mod, x, z
+    f64, j64, x64, t64, s64 = res["fp64"]
+    fmx, jmx, xmx, tmx, smx = res["mixed"]
+    out.update({"rel_dlogL": abs(fmx - f64) / abs(f64), "rel_dgrad": float(np.abs(jmx - j64).max() / np.abs(j64).max()),
+                "rel_dsamples": float(np.abs(xmx - x64).max() / np.abs(x64).max()),
+                "eval_s": {"fp64": round(t64, 3), "mixed": round(tmx, 3)},
+                "sample256_s": {"fp64": round(s64, 3), "mixed": round(smx, 3)}})
+    return out
+
+
 def replica_throughput(local_ms, steps, world, dist=None, device="cpu"):
     """Whole-job evaluations/s of `world` independent replicas that each ran
     `steps` evaluations in `local_ms`: the job time is the slowest rank's (max
@@ -302,6 +342,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-pcg", action="store_true")
     ap.add_argument("--fit", action="store_true", help="also run the L-BFGS fit on the sensor-track workload")
+    ap.add_argument("--config2", action="store_true", help="also compare mixed and FP64 plans at 100x100x24")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -419,6 +460,7 @@ def main():
     cb = None if args.no_cpu else cpu_baseline()
     pcg = None if args.no_pcg else learned_pcg_leg()
     fit = lbfgs_fit_leg() if args.fit else None
+    c2 = config2_leg() if args.config2 else None
     nobs = int(w.idx.size)
     line = {
         "metric": METRIC, "value": evals_per_s, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
@@ -450,7 +492,7 @@ def main():
         "algorithmic": {"factor_tflop": info.factor_flops / 1e12, "selinv_tflop": info.selinv_flops / 1e12,
                         "nnz_L": info.nnz_l},
         "gemm_sites": sites,
-        "objective": f, "clocks": clk, "cpu_baseline": cb, "fp64_plain": fp64, "learned_pcg": pcg, "lbfgs_fit": fit,
+        "objective": f, "clocks": clk, "cpu_baseline": cb, "fp64_plain": fp64, "learned_pcg": pcg, "lbfgs_fit": fit, "stationary_100x100x24": c2,
     }
     print(json.dumps(line))
 
