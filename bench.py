@@ -378,7 +378,7 @@ def main():
     torch.cuda.synchronize()
     L = nat.lib()
     L.spde_plan_read_profile(plan.h, None, None, None, 1)
-    L.spde_plan_set_profiling(plan.h, 1)
+    L.spde_plan_set_profiling(plan.h, 2)  # events around the tensor-core products only
     launches0 = plan.info().launches
     clocks = Clocks()
     clocks.start()
@@ -396,18 +396,24 @@ def main():
     torch.cuda.synchronize()
     evals_per_s, ms = replica_throughput(e0.elapsed_time(e1), args.steps, world, dist, "cuda")
     clk = clocks.stop()
-    L.spde_plan_set_profiling(plan.h, 0)
     launches = plan.info().launches - launches0
     pms, pfl, pct = (np.zeros(10), np.zeros(10), np.zeros(10, dtype=np.int64))
     L.spde_plan_read_profile(plan.h, pms.ctypes.data, pfl.ctypes.data, pct.ctypes.data, 1)
+    L.spde_plan_read_sites(plan.h, None, None, None, 1)
+    # one more pass with every launch timed, for the split by kernel class and call site
+    L.spde_plan_set_profiling(plan.h, 1)
+    evaluate()
+    L.spde_plan_set_profiling(plan.h, 0)
+    cms, cfl, cct = (np.zeros(10), np.zeros(10), np.zeros(10, dtype=np.int64))
+    L.spde_plan_read_profile(plan.h, cms.ctypes.data, cfl.ctypes.data, cct.ctypes.data, 1)
     sms, sfl, stl = np.zeros(18), np.zeros(18), np.zeros(18, dtype=np.int64)
     L.spde_plan_read_sites(plan.h, sms.ctypes.data, sfl.ctypes.data, stl.ctypes.data, 1)
     site_names = ["", "factor_panel_solve", "factor_panel_update", "factor_schur", "fwd_diag", "fwd_below", "fwd_border",
                   "bwd_border", "bwd_diag", "bwd_above", "inv_x_solve", "inv_x_update", "inv_zbs", "inv_xj", "inv_zrj",
                   "inv_zjj", "inv_zjj2", "inv_zss"]
-    sites = {site_names[i]: {"ms": round(float(sms[i] / args.steps), 3),
+    sites = {site_names[i]: {"ms": round(float(sms[i]), 3),
                              "tflops": round(float(sfl[i] / max(sms[i], 1e-9) / 1e9), 2),
-                             "tiles": int(stl[i] // args.steps)} for i in range(1, 18) if sms[i] > 0}
+                             "tiles": int(stl[i])} for i in range(1, 18) if sms[i] > 0}
 
     # end to end through the public API: host data in, host objective/gradient out
     torch.cuda.synchronize()
@@ -481,12 +487,13 @@ def main():
                      "traffic_source": "ncu dram bytes per flop of two captured launches (100x100x24), "
                                        "scaled by this run's flops per launch",
                      "launches_per_step": float(pct[9] / args.steps),
-                     "note": "launch durations measured while the Q and Q + tau S^T S pipelines run concurrently "
-                             "on two streams (per-class times below are summed over both)",
+                     "note": "CUDA events around each tensor-core launch in the timed region, while the Q and "
+                             "Q + tau S^T S pipelines run concurrently on two streams; the per-class split below "
+                             "comes from one extra evaluation with every launch timed, summed over both streams",
                      "share_of_step": tc_ms / (ms / args.steps),
                      "tf32_cublas_tflops": tf32,
                      "frac_of_3xtf32": achieved / (tf32 / 3.0) if tf32 else None},
-        "profile_ms_per_step": {k: float(pms[i] / args.steps) for i, k in enumerate(
+        "profile_ms_per_step": {k: float(cms[i]) for i, k in enumerate(
             ["memset", "extend_add", "diag_block", "product_cuda_cores", "fwd_gather", "bwd_gather", "inv_gather",
              "transpose", "inv_extract", "product_tensor_cores"])},
         "algorithmic": {"factor_tflop": info.factor_flops / 1e12, "selinv_tflop": info.selinv_flops / 1e12,

@@ -103,7 +103,8 @@ int spde_plan_set_stream(SpdePlan* plan, void* stream);
 int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info);
 const char* spde_last_error(const SpdePlan* plan);
 /* Optional per-launch timing with CUDA events on the plan's stream (no
- * reference counterpart; measurement only).  read_profile fills 10 entries per
+ * reference counterpart; measurement only): enable 1 times every launch, 2 only
+ * the tensor-core products, 0 none.  read_profile fills 10 entries per
  * launch class (0 memset, 1 extend-add, 2 diagonal block, 3 tiled product on
  * the CUDA cores, 4 forward gather, 5 backward gather, 6 inverse gather,
  * 7 transpose, 8 inverse extraction, 9 tiled product on the tensor cores):

@@ -284,6 +284,7 @@ static void share_model(const Plan& p, Plan& t) {
   t.d_obs_idx = p.d_obs_idx;
   t.nobs = p.nobs;
   t.profile = p.profile;
+  t.profile_tc_only = p.profile_tc_only;
 }
 
 static int no_factor(SpdePlan* plan) {
@@ -365,11 +366,13 @@ const char* spde_last_error(const SpdePlan* plan) { return plan ? plan->p.last_e
 
 int spde_plan_set_profiling(SpdePlan* plan, int enable) {
   if (!plan) return SPDE_ERR_ARG;
-  prof_collect(&plan->p);
-  plan->p.profile = enable != 0;
-  if (plan->twin) {
-    prof_collect(plan->twin.get());
-    plan->twin->profile = enable != 0;
+  if (enable < 0 || enable > 2) return SPDE_ERR_ARG;
+  Plan* ps[2] = {&plan->p, plan->twin.get()};
+  for (Plan* q : ps) {
+    if (!q) continue;
+    prof_collect(q);
+    q->profile = enable != 0;
+    q->profile_tc_only = enable == 2;
   }
   return SPDE_OK;
 }

@@ -843,8 +843,8 @@ struct Exec {
   void run() {
     cudaStream_t st = p->stream;
     for (const Op& o : s.ops) {
-      const bool timed = p->profile && o.kind != OP_MEMSET;
       const bool on_tc = o.kind == OP_GEMM && sizeof(T) == sizeof(float) && o.tc == kPathTensor && tc_gemm_enabled();
+      const bool timed = p->profile && o.kind != OP_MEMSET && (on_tc || !p->profile_tc_only);
       if (timed) prof_begin(p, st);
       switch (o.kind) {
         case OP_MEMSET: cudaMemsetAsync(buf(o.cbuf), 0, size_t(o.elems) * sizeof(T), st); break;

@@ -124,6 +124,7 @@ struct Plan {
   // counters and optional per-launch timing (CUDA events on the plan's stream)
   int64_t launches_total = 0;
   bool profile = false;
+  bool profile_tc_only = false;  // time only the tensor-core products
   std::vector<cudaEvent_t> ev_pool;
   std::vector<std::pair<int, double>> ev_pending;  // (op kind, flops) per recorded pair
   size_t ev_used = 0;
