@@ -258,7 +258,11 @@ static int ensure_twin(SpdePlan* plan) {
   if (!t) return SPDE_ERR_NO_MEMORY;
   t->precision = p.precision;
   t->sym = p.sym;
-  if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  // the second pipeline carries the conditional-mean solve, a chain of small
+  // latency-bound launches on the evaluation's critical path: highest priority
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (cudaStreamCreateWithPriority(&t->stream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
     p.last_error = "could not create the second pipeline's stream";
     return SPDE_ERR_CUDA;
   }
