@@ -104,88 +104,182 @@ static void gemm_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, in
 }
 
 // ------------------------------------------------------------ narrow GEMM
-// Products with at most kNarrowN output columns (solves with few right-hand
-// sides) are bandwidth work: one CTA per task streams its (<= 128) A rows once,
-// coalesced, against B staged in shared memory, instead of computing a mostly
-// empty 128 x 128 register tile.  The block reads all of its A and B before it
+// Products with at most 8 output columns (solves with few right-hand sides) are
+// bandwidth work: one CTA per task (m <= 128 rows) streams its A once,
+// coalesced, against B staged in shared memory.  Each thread keeps 16 to 32
+// independent loads in flight, and the CTA holds only 8 KB of shared memory
+// (FP32), so that it fits on an SM beside a resident tensor-core CTA.  NB (1 or
+// 8) bounds the task's columns.  Every CTA reads all of its A and B before it
 // writes C (in-place solves stay valid).
 constexpr int kNarrowN = 8;
-constexpr int kNarrowSmem = 24 * 1024;  // staged B (k x 8 columns) per chunk
+constexpr int kNarrowBEnt = 2048;  // shared entries: staged B (NB x k chunk), then the k-split partial sums
 
-template <typename T, int MODE, int AL, int BL>
+// Sum of v[r] over the 32 lanes of the warp for the eight rows r: lanes with
+// (lane >> 2) == r receive row r (a butterfly that halves the rows each lane
+// carries at every step: 9 shuffles instead of 8 x 5).
+template <typename T>
+__device__ __forceinline__ T warp_sum8(const T (&v)[8], int lane) {
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  T w[4], x[2];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const T send = b4 ? v[r] : v[r + 4], keep = b4 ? v[r + 4] : v[r];
+    w[r] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const T send = b3 ? w[r] : w[r + 2], keep = b3 ? w[r + 2] : w[r];
+    x[r] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  T y = (b2 ? x[1] : x[0]) + __shfl_xor_sync(0xffffffffu, b2 ? x[0] : x[1], 4);
+  y += __shfl_xor_sync(0xffffffffu, y, 2);
+  y += __shfl_xor_sync(0xffffffffu, y, 1);
+  return y;
+}
+
+template <int MODE, typename T>
+__device__ __forceinline__ void narrow_store(T* dst, T v) {
+  if (MODE == kSub) *dst -= v;
+  else if (MODE == kStore) *dst = v;
+  else if (MODE == kNegStore) *dst = -v;
+  else *dst += v;
+}
+
+template <typename T, int MODE, int AL, int NB>
 __global__ void __launch_bounds__(256) gemv_kernel(const GemmTask* __restrict__ tasks, const T* Ab, const T* Bb,
-                                                   T* Cb) {
-  constexpr int kBEnt = kNarrowSmem / int(sizeof(T));  // staged B entries (k x n)
-  __shared__ T Bs[kBEnt];
-  __shared__ T acc_s[2][128][kNarrowN];
+                                                   T* Cb, int bl) {
+  constexpr int kc = kNarrowBEnt / NB;  // k values per staged chunk (a multiple of 64)
+  __shared__ T sh[kNarrowBEnt];         // Bs[j * kc + kk] while streaming, partial sums after
   const GemmTask tk = tasks[blockIdx.x];
   const T* A = Ab + tk.a;
   const T* B = Bb + tk.b;
   T* C = Cb + tk.c;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n = tk.n, m = tk.m;
-  const int kc = kBEnt / kNarrowN;  // k values per chunk
-  T s[kNarrowN];
+  if (AL == kRow) {
+    // rows in batches of 8; warp w owns batches w and w + 8 (m <= 128); lanes
+    // stride along k, 64 k values per step
+    constexpr int BAT = NB == 1 ? 2 : 1;  // batches loaded together
+    T res[2][NB];
 #pragma unroll
-  for (int j = 0; j < kNarrowN; ++j) s[j] = T(0);
-  for (int e = tid; e < 2 * 128 * kNarrowN; e += 256) (&acc_s[0][0][0])[e] = T(0);
-  for (int k0 = 0; k0 < tk.k; k0 += kc) {
-    const int kn = min(kc, tk.k - k0);
-    __syncthreads();
-    for (int e = tid; e < kn * n; e += 256) {
-      int kk, j;
-      if (BL == kRow) { j = e / kn; kk = e - j * kn; } else { kk = e / n; j = e - kk * n; }
-      Bs[kk * kNarrowN + j] = BL == kRow ? B[int64_t(j) * tk.ldb + k0 + kk] : B[int64_t(k0 + kk) * tk.ldb + j];
+    for (int q = 0; q < 2; ++q)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) res[q][j] = T(0);
+    for (int k0 = 0; k0 < tk.k; k0 += kc) {
+      const int kn = min(kc, tk.k - k0);
+      const int kp = (kn + 63) & ~63;
+      __syncthreads();
+      for (int e = tid; e < kp * NB; e += 256) {
+        const int j = e / kp, kk = e - j * kp;
+        T v = T(0);
+        if (kk < kn && j < n) v = bl == kRow ? B[int64_t(j) * tk.ldb + k0 + kk] : B[int64_t(k0 + kk) * tk.ldb + j];
+        sh[j * kc + kk] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int b0 = 0; b0 < 2; b0 += BAT) {
+        if (8 * (warp + 8 * b0) >= m) break;
+        T v[BAT][8][NB];
+#pragma unroll
+        for (int q = 0; q < BAT; ++q)
+#pragma unroll
+          for (int r = 0; r < 8; ++r)
+#pragma unroll
+            for (int j = 0; j < NB; ++j) v[q][r][j] = T(0);
+        for (int kk0 = 0; kk0 < kn; kk0 += 64) {
+          T a[BAT][8][2];
+#pragma unroll
+          for (int q = 0; q < BAT; ++q)
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+              const int i = 8 * (warp + 8 * (b0 + q)) + r;
+              const T* ar = A + int64_t(i) * tk.lda + k0 + kk0 + lane;
+#pragma unroll
+              for (int u = 0; u < 2; ++u)
+                a[q][r][u] = (i < m && kk0 + lane + 32 * u < kn) ? ar[32 * u] : T(0);
+            }
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            T bv[NB];
+#pragma unroll
+            for (int j = 0; j < NB; ++j) bv[j] = sh[j * kc + kk0 + lane + 32 * u];
+#pragma unroll
+            for (int q = 0; q < BAT; ++q)
+#pragma unroll
+              for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int j = 0; j < NB; ++j) v[q][r][j] = fma(a[q][r][u], bv[j], v[q][r][j]);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < BAT; ++q)
+#pragma unroll
+          for (int j = 0; j < NB; ++j) {
+            T col[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) col[r] = v[q][r][j];
+            res[b0 + q][j] += warp_sum8(col, lane);
+          }
+      }
     }
     __syncthreads();
-    if (AL == kRow) {
-      // warp w owns rows w, w + 8, ...; lanes stride along the row
-      for (int i = warp; i < m; i += 8) {
-        T p[kNarrowN];
+    if ((lane & 3) == 0) {
 #pragma unroll
-        for (int j = 0; j < kNarrowN; ++j) p[j] = T(0);
-        const T* ar = A + int64_t(i) * tk.lda + k0;
-        for (int kk = lane; kk < kn; kk += 32) {
-          const T a = ar[kk];
+      for (int q = 0; q < 2; ++q) {
+        const int i = 8 * (warp + 8 * q) + (lane >> 2);
+        if (i < m) {
 #pragma unroll
-          for (int j = 0; j < kNarrowN; ++j)
-            if (j < n) p[j] = fma(a, Bs[kk * kNarrowN + j], p[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < kNarrowN; ++j) {
-          if (j >= n) break;
-          T v = p[j];
-          for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-          if (lane == 0) acc_s[0][i][j] += v;
+          for (int j = 0; j < NB; ++j)
+            if (j < n) narrow_store<MODE>(C + int64_t(i) * tk.ldc + j, res[q][j]);
         }
       }
-    } else {
-      // thread (h, i): row i, every other k starting at h
-      const int i = tid & 127, h = tid >> 7;
+    }
+  } else {
+    // thread (h, i): row i, every H-th k value starting at h; 8 loads in flight
+    const int rsh = m <= 32 ? 5 : (m <= 64 ? 6 : 7);
+    const int i = tid & ((1 << rsh) - 1), h = tid >> rsh, H = 256 >> rsh;
+    T s[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) s[j] = T(0);
+    for (int k0 = 0; k0 < tk.k; k0 += kc) {
+      const int kn = min(kc, tk.k - k0);
+      __syncthreads();
+      for (int e = tid; e < kn * NB; e += 256) {
+        const int j = e / kn, kk = e - j * kn;
+        T v = T(0);
+        if (j < n) v = bl == kRow ? B[int64_t(j) * tk.ldb + k0 + kk] : B[int64_t(k0 + kk) * tk.ldb + j];
+        sh[j * kc + kk] = v;
+      }
+      __syncthreads();
       if (i < m) {
-        for (int kk = h; kk < kn; kk += 2) {
-          const T a = A[int64_t(k0 + kk) * tk.lda + i];
+        const T* ac = A + int64_t(k0) * tk.lda + i;
+        int kk = h;
+        for (; kk + 7 * H < kn; kk += 8 * H) {
+          T a[8];
 #pragma unroll
-          for (int j = 0; j < kNarrowN; ++j)
-            if (j < n) s[j] = fma(a, Bs[kk * kNarrowN + j], s[j]);
+          for (int u = 0; u < 8; ++u) a[u] = ac[int64_t(kk + u * H) * tk.lda];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+#pragma unroll
+            for (int j = 0; j < NB; ++j) s[j] = fma(a[u], sh[j * kc + kk + u * H], s[j]);
+        }
+        for (; kk < kn; kk += H) {
+          const T a = ac[int64_t(kk) * tk.lda];
+#pragma unroll
+          for (int j = 0; j < NB; ++j) s[j] = fma(a, sh[j * kc + kk], s[j]);
         }
       }
     }
-  }
-  if (AL == kCol) {
-    const int i = tid & 127, h = tid >> 7;
+    __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kNarrowN; ++j) acc_s[h][i][j] = s[j];
-  }
-  __syncthreads();
-  for (int e = tid; e < m * n; e += 256) {
-    const int i = e / n, j = e - i * n;
-    const T v = AL == kCol ? acc_s[0][i][j] + acc_s[1][i][j] : acc_s[0][i][j];
-    T* dst = C + int64_t(i) * tk.ldc + j;
-    if (MODE == kSub) *dst -= v;
-    else if (MODE == kStore) *dst = v;
-    else if (MODE == kNegStore) *dst = -v;
-    else *dst += v;
+    for (int j = 0; j < NB; ++j) sh[j * 256 + tid] = s[j];
+    __syncthreads();
+    for (int e = tid; e < m * n; e += 256) {
+      const int ii = e / n, j = e - ii * n;
+      T v = T(0);
+      for (int hh = 0; hh < H; ++hh) v += sh[j * 256 + (hh << rsh) + ii];
+      narrow_store<MODE>(C + int64_t(ii) * tk.ldc + j, v);
+    }
   }
 }
 
@@ -263,11 +357,15 @@ static void panel64_launch(const GemmTask* t, int n, const float* A, const float
 }
 
 template <typename T, int MODE>
-static void gemv_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, int al, int bl, cudaStream_t st) {
-  if (al == kRow && bl == kRow) gemv_kernel<T, MODE, kRow, kRow><<<n, 256, 0, st>>>(t, A, B, C);
-  else if (al == kRow && bl == kCol) gemv_kernel<T, MODE, kRow, kCol><<<n, 256, 0, st>>>(t, A, B, C);
-  else if (al == kCol && bl == kRow) gemv_kernel<T, MODE, kCol, kRow><<<n, 256, 0, st>>>(t, A, B, C);
-  else gemv_kernel<T, MODE, kCol, kCol><<<n, 256, 0, st>>>(t, A, B, C);
+static void gemv_mode(const GemmTask* t, int n, const T* A, const T* B, T* C, int al, int bl, cudaStream_t st,
+                      int nmax) {
+  if (nmax == 1) {
+    if (al == kRow) gemv_kernel<T, MODE, kRow, 1><<<n, 256, 0, st>>>(t, A, B, C, bl);
+    else gemv_kernel<T, MODE, kCol, 1><<<n, 256, 0, st>>>(t, A, B, C, bl);
+  } else {
+    if (al == kRow) gemv_kernel<T, MODE, kRow, kNarrowN><<<n, 256, 0, st>>>(t, A, B, C, bl);
+    else gemv_kernel<T, MODE, kCol, kNarrowN><<<n, 256, 0, st>>>(t, A, B, C, bl);
+  }
 }
 
 // The FP32 products run on the tensor cores unless SPDE_TC=0 is set in the environment.
@@ -282,14 +380,14 @@ bool tc_gemm_enabled() {
 
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout, int blayout,
-                 cudaStream_t st, int path) {
+                 cudaStream_t st, int path, int nmax) {
   if (ntasks <= 0) return;
   if (path == kPathNarrow) {
     switch (mode) {
-      case kSub: gemv_mode<T, kSub>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
-      case kStore: gemv_mode<T, kStore>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
-      case kNegStore: gemv_mode<T, kNegStore>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
-      default: gemv_mode<T, kAdd>(tasks, ntasks, A, B, C, alayout, blayout, st); break;
+      case kSub: gemv_mode<T, kSub>(tasks, ntasks, A, B, C, alayout, blayout, st, nmax); break;
+      case kStore: gemv_mode<T, kStore>(tasks, ntasks, A, B, C, alayout, blayout, st, nmax); break;
+      case kNegStore: gemv_mode<T, kNegStore>(tasks, ntasks, A, B, C, alayout, blayout, st, nmax); break;
+      default: gemv_mode<T, kAdd>(tasks, ntasks, A, B, C, alayout, blayout, st, nmax); break;
     }
     return;
   }
@@ -321,9 +419,9 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
 }
 
 template void launch_gemm<double>(const GemmTask*, int, const double*, const double*, double*, int, int, int,
-                                  cudaStream_t, int);
+                                  cudaStream_t, int, int);
 template void launch_gemm<float>(const GemmTask*, int, const float*, const float*, float*, int, int, int,
-                                 cudaStream_t, int);
+                                 cudaStream_t, int, int);
 
 // --------------------------------------------------- diagonal block POTRF
 // Cholesky factor and inverse of one w x w diagonal block (w <= 64) per CTA.
@@ -548,6 +646,19 @@ __device__ __forceinline__ DF df_rcp(DF d) {
   return df_renorm(r, __fmul_rn(r, one_minus.hi));
 }
 
+// 1 / sqrt(d) rounded to FP32 for a double-float pivot: the FP32 estimate
+// refined by one Newton-Raphson step y (3 - d y^2) / 2 in FP64, which leaves an
+// error far below FP32 rounding (L and L^-1 are stored in FP32).
+__device__ __forceinline__ float df_rsqrt(DF d) {
+  const double x = double(d.hi) + double(d.lo);
+  const double y = rsqrtf(d.hi + d.lo);
+  return float(y * (1.5 - 0.5 * x * y * y));
+}
+
+// The inverse's forward elimination runs one step behind the factorisation in
+// the same barrier interval: step s factors column s (publishing column s + 1),
+// writes the finished column s of L, and eliminates with column s - 1 of L and
+// row s - 1 of L^-1 (publishing row s), so a block takes w + 1 barriers.
 __global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restrict__ tasks, float* __restrict__ L,
                                                        float* __restrict__ dinv, double* __restrict__ logpiv,
                                                        int* __restrict__ err) {
@@ -570,8 +681,13 @@ __global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restric
       const int i = ty + 16 * m, k = tx + 16 * n;
       r[m][n] = DF{(k <= i && i < w) ? blk[int64_t(i) * tk.lda + k] : 0.0f, 0.0f};
     }
+  float b[4][4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) b[m][n] = (ty + 16 * m == tx + 16 * n) ? 1.0f : 0.0f;
   if (tid == 0) bad = 0;
-  // publish column 0 and its pivot reciprocal
+  // publish column 0, its pivot and 1 / L_00; row 0 of L^-1 is (1 / L_00, 0, ...)
   if (tx == 0) {
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
@@ -583,61 +699,125 @@ __global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restric
         const DF q = df_rcp(d);
         dvh[0] = q.hi; dvl[0] = q.lo;
         dpiv[0] = double(d.hi) + double(d.lo);
+        const float rs = df_rsqrt(d);
+        rsq[0] = rs;
+        b[0][0] = rs;
+        xrow[0][0] = rs;
       }
     }
   }
   __syncthreads();
-  for (int j = 0; j < w; ++j) {
-    const float* ch = colh[j & 1];
-    const float* cl = coll[j & 1];
-    const DF dv{dvh[j], dvl[j]};
-    DF ci[4], ck[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      const int i = ty + 16 * m;
-      ci[m] = (i > j && i < w) ? df_mul(DF{ch[i], cl[i]}, dv) : DF{0.0f, 0.0f};
-    }
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const int k = tx + 16 * n;
-      ck[n] = (k > j && k < w) ? DF{ch[k], cl[k]} : DF{0.0f, 0.0f};
-    }
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      if (16 * m + 15 <= j) continue;
-#pragma unroll
-      for (int n = 0; n <= m; ++n) {
-        if (16 * n + 15 <= j) continue;
-        r[m][n] = df_fms(r[m][n], ci[m], ck[n]);
-      }
-    }
-    // publish column j + 1; the owner of its diagonal also publishes the pivot
-    const int jn = j + 1;
-    if (jn < w && tx == (jn & 15)) {
-      const int n = jn >> 4;
+  for (int st = 0; st <= w; ++st) {
+    if (st < w) {
+      // ---- factorisation step j = st
+      const int j = st;
+      const float* ch = colh[j & 1];
+      const float* cl = coll[j & 1];
+      const DF dv{dvh[j], dvl[j]};
+      DF ci[4], ck[4];
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
         const int i = ty + 16 * m;
-        if (i >= jn && i < w) {
+        ci[m] = (i > j && i < w) ? df_mul(DF{ch[i], cl[i]}, dv) : DF{0.0f, 0.0f};
+      }
 #pragma unroll
-          for (int nn = 0; nn < 4; ++nn)
-            if (nn == n) {
-              colh[jn & 1][i] = r[m][nn].hi;
-              coll[jn & 1][i] = r[m][nn].lo;
-              if (i == jn) {
-                DF d = r[m][nn];
-                if (!(d.hi > 0.0f) || !isfinite(d.hi)) { d = DF{1.0f, 0.0f}; bad = 1; }
-                const DF q = df_rcp(d);
-                dvh[jn] = q.hi; dvl[jn] = q.lo;
-                dpiv[jn] = double(d.hi) + double(d.lo);
+      for (int n = 0; n < 4; ++n) {
+        const int k = tx + 16 * n;
+        ck[n] = (k > j && k < w) ? DF{ch[k], cl[k]} : DF{0.0f, 0.0f};
+      }
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        if (16 * m + 15 <= j) continue;
+#pragma unroll
+        for (int n = 0; n <= m; ++n) {
+          if (16 * n + 15 <= j) continue;
+          r[m][n] = df_fms(r[m][n], ci[m], ck[n]);
+        }
+      }
+      // column j of L is final: L_ij = a_ij / sqrt(d_j) (threads 0..63 by row)
+      if (tid < w) {
+        const int i = tid;
+        float v = 0.0f;
+        if (i == j) v = 1.0f / rsq[j];
+        else if (i > j) v = (ch[i] + cl[i]) * rsq[j];
+        lsh[i][j] = v;
+      }
+      // publish column j + 1; the owner of its diagonal also publishes the pivot
+      const int jn = j + 1;
+      if (jn < w && tx == (jn & 15)) {
+        const int n = jn >> 4;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const int i = ty + 16 * m;
+          if (i >= jn && i < w) {
+#pragma unroll
+            for (int nn = 0; nn < 4; ++nn)
+              if (nn == n) {
+                colh[jn & 1][i] = r[m][nn].hi;
+                coll[jn & 1][i] = r[m][nn].lo;
+                if (i == jn) {
+                  DF d = r[m][nn];
+                  if (!(d.hi > 0.0f) || !isfinite(d.hi)) { d = DF{1.0f, 0.0f}; bad = 1; }
+                  const DF q = df_rcp(d);
+                  dvh[jn] = q.hi; dvl[jn] = q.lo;
+                  dpiv[jn] = double(d.hi) + double(d.lo);
+                  rsq[jn] = df_rsqrt(d);
+                }
               }
+          }
+        }
+      }
+    }
+    if (st >= 1) {
+      // ---- elimination step j = st - 1 of X = L^-1: B_ic -= L_ij X_jc (i > j, c <= j),
+      // then row j + 1 of X is finished: B_(j+1)c / L_(j+1)(j+1)
+      const int j = st - 1;
+      const float* xr = xrow[j & 1];
+      float li[4], xc[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const int i = ty + 16 * m;
+        li[m] = (i > j && i < w) ? lsh[i][j] : 0.0f;
+      }
+#pragma unroll
+      for (int n = 0; n < 4; ++n) {
+        const int cc = tx + 16 * n;
+        xc[n] = cc <= j ? xr[cc] : 0.0f;
+      }
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        if (16 * m + 15 <= j) continue;
+#pragma unroll
+        for (int n = 0; n <= m; ++n) {
+          if (16 * n > j) continue;
+          b[m][n] = fmaf(-li[m], xc[n], b[m][n]);
+        }
+      }
+      const int jn = j + 1;
+      if (jn < w && ty == (jn & 15)) {
+        const int m = jn >> 4;
+        const float inv = rsq[jn];
+#pragma unroll
+        for (int mm = 0; mm < 4; ++mm) {
+          if (mm != m) continue;
+#pragma unroll
+          for (int n = 0; n < 4; ++n) {
+            const int cc = tx + 16 * n;
+            if (cc <= jn) {
+              b[mm][n] *= inv;
+              xrow[jn & 1][cc] = b[mm][n];
             }
+          }
         }
       }
     }
     __syncthreads();
   }
-  if (tid < w) rsq[tid] = float(1.0 / sqrt(dpiv[tid]));
+  // L (zero above the diagonal) back to the block, row-contiguous
+  for (int e = tid; e < w * w; e += 256) {
+    const int i = e / w, k = e - i * w;
+    blk[int64_t(i) * tk.lda + k] = k <= i ? lsh[i][k] : 0.0f;
+  }
   if (tid < 32) {
     double sum = 0.0;
     for (int j = tid; j < w; j += 32) sum += 0.5 * log(dpiv[j]);
@@ -646,70 +826,6 @@ __global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restric
       logpiv[blockIdx.x] = sum;
       if (bad) atomicCAS(err, -1, tk.front);
     }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int m = 0; m < 4; ++m)
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const int i = ty + 16 * m, k = tx + 16 * n;
-      if (i < w && k < w) {
-        const float v = k < i ? (r[m][n].hi + r[m][n].lo) * rsq[k] : (k == i ? 1.0f / rsq[k] : 0.0f);
-        lsh[i][k] = v;
-        blk[int64_t(i) * tk.lda + k] = v;
-      }
-    }
-  float b[4][4];
-#pragma unroll
-  for (int m = 0; m < 4; ++m)
-#pragma unroll
-    for (int n = 0; n < 4; ++n) b[m][n] = (ty + 16 * m == tx + 16 * n) ? 1.0f : 0.0f;
-  __syncthreads();
-  if (ty == 0 && tx == 0) {
-    b[0][0] = 1.0f / lsh[0][0];
-    xrow[0][0] = b[0][0];
-  }
-  __syncthreads();
-  for (int j = 0; j < w; ++j) {
-    const float* xr = xrow[j & 1];
-    float li[4], xc[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      const int i = ty + 16 * m;
-      li[m] = (i > j && i < w) ? lsh[i][j] : 0.0f;
-    }
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const int cc = tx + 16 * n;
-      xc[n] = cc <= j ? xr[cc] : 0.0f;
-    }
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      if (16 * m + 15 <= j) continue;
-#pragma unroll
-      for (int n = 0; n <= m; ++n) {
-        if (16 * n > j) continue;
-        b[m][n] = fmaf(-li[m], xc[n], b[m][n]);
-      }
-    }
-    const int jn = j + 1;
-    if (jn < w && ty == (jn & 15)) {
-      const int m = jn >> 4;
-      const float inv = 1.0f / lsh[jn][jn];
-#pragma unroll
-      for (int mm = 0; mm < 4; ++mm) {
-        if (mm != m) continue;
-#pragma unroll
-        for (int n = 0; n < 4; ++n) {
-          const int cc = tx + 16 * n;
-          if (cc <= jn) {
-            b[mm][n] *= inv;
-            xrow[jn & 1][cc] = b[mm][n];
-          }
-        }
-      }
-    }
-    __syncthreads();
   }
   float* dvp = dinv + tk.dinv;
 #pragma unroll

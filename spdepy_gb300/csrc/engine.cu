@@ -86,10 +86,11 @@ struct Builder {
   void split_by_k() {
     Op& o = s.ops.back();
     const int64_t beg = o.off, end = int64_t(s.gemm.size());
-    bool narrow = end > beg;
-    for (int64_t i = beg; i < end && narrow; ++i) narrow = s.gemm[i].n <= kNarrowMaxN;
-    if (narrow) {
+    int nmax = 0;
+    for (int64_t i = beg; i < end; ++i) nmax = std::max(nmax, s.gemm[i].n);
+    if (end > beg && nmax <= kNarrowMaxN) {
       o.tc = kPathNarrow;
+      o.nmax = nmax;
       return;
     }
     // panel solves, and look-ahead updates of one block column: m <= TM, n <= 64, k <= 64
@@ -857,7 +858,7 @@ struct Exec {
           break;
         case OP_GEMM:
           launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st,
-                         o.tc);
+                         o.tc, o.nmax);
           if (on_tc) tc_launch_log(o);
           break;
         case OP_SGATHER_FWD: {

@@ -36,6 +36,7 @@ struct Op {
   double flops = 0.0;  // algorithmic flops of a GEMM launch (2 m n k summed over its tiles)
   int site = 0;
   int tc = 1;          // product path (GemmPath): CUDA-core tiles, tensor-core tiles (FP32), narrow
+  int nmax = 0;        // largest task n of a narrow launch
   int kind = 0;
   int64_t off = 0;  // first task in the array of this kind
   int count = 0;

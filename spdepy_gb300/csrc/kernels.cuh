@@ -46,9 +46,10 @@ struct DevFront {
 enum GemmPath { kPathSimt = 0, kPathTensor = 1, kPathNarrow = 2, kPathPanel = 3 };
 constexpr int kNarrowMaxN = 8;
 
+// nmax bounds the tasks' n on the narrow path (1 selects the one-column kernel).
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout,
-                 int blayout, cudaStream_t st, int path = kPathTensor);
+                 int blayout, cudaStream_t st, int path = kPathTensor, int nmax = kNarrowMaxN);
 
 // tcgen05 path for FP32 (tc_gemm.cu); tc_gemm_take_error returns and clears the
 // bounded-wait error flag of that kernel.

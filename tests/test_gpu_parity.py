@@ -135,6 +135,26 @@ def test_solve_refinement_and_sample_identity():
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("nrhs", [1, 2, 8])
+def test_narrow_solves(precision, nrhs):
+    """Solves with at most 8 right-hand sides run on the narrow products (the
+    one-column kernel for nrhs = 1): Q x = b to the refinement tolerance, and
+    each column equals the same solve done alone."""
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, precision)
+    mod._assemble(g["par"])
+    plan = mod.plan
+    plan.factor(False, 0.0)
+    n = mod.grid.n
+    b = torch.randn(n, nrhs, dtype=torch.float64, generator=torch.Generator().manual_seed(nrhs))
+    x, res = plan.solve(b, refine=10, tol=1e-12)
+    assert res < 1e-10
+    assert torch.allclose(plan.spmv(x).cpu(), b, rtol=0, atol=1e-9 * b.abs().max())
+    x1, _ = plan.solve(b[:, -1:].contiguous(), refine=10, tol=1e-12)
+    assert torch.allclose(x[:, -1:].cpu(), x1.cpu(), rtol=0, atol=1e-9 * x1.abs().max().item())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_selected_inverse_vs_dense(precision):
     g = load("covadv_vardiff_bc1")
     mod = gpu_model(g, precision)
