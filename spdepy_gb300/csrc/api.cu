@@ -3,6 +3,9 @@
 #include <math.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <mutex>
 #include <cstring>
 #include <string>
 #include <memory>
@@ -157,6 +160,46 @@ double host_sum_partials(const double* dpart, int nblk, cudaStream_t st) {
 int ntheta_of(const Plan& p) { return 4 * p.model.nk + p.model.nw + 6; }
 
 }  // namespace
+
+// Optional phase timeline of spde_loglike: with SPDE_PHASE_LOG set, the end of
+// each phase of the two pipelines (factor, solve, inverse) is recorded with a
+// CUDA event on the phase's stream and printed to stderr in ms from the end of
+// the assembly.
+struct PhaseLog {
+  bool on = false;
+  cudaEvent_t t0 = nullptr;
+  std::vector<std::pair<const char*, cudaEvent_t>> marks;
+  std::mutex mu;
+  explicit PhaseLog(cudaStream_t st) {
+    on = std::getenv("SPDE_PHASE_LOG") != nullptr;
+    if (!on) return;
+    cudaEventCreate(&t0);
+    cudaEventRecord(t0, st);
+  }
+  void mark(const char* what, cudaStream_t st) {
+    if (!on) return;
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, st);
+    std::lock_guard<std::mutex> g(mu);
+    marks.emplace_back(what, e);
+  }
+  ~PhaseLog() {
+    if (!on) return;
+    std::string line = "phases (ms):";
+    for (auto& m : marks) {
+      float ms = 0.0f;
+      cudaEventSynchronize(m.second);
+      cudaEventElapsedTime(&ms, t0, m.second);
+      char buf[96];
+      std::snprintf(buf, sizeof(buf), " %s %.2f", m.first, ms);
+      line += buf;
+      cudaEventDestroy(m.second);
+    }
+    cudaEventDestroy(t0);
+    std::fprintf(stderr, "%s\n", line.c_str());
+  }
+};
 
 struct LoglikeScratch {
   DevBuf zq, zqc, b, mu, qmu, part, gbar, gradv, work, trq, trc, d;
@@ -657,15 +700,19 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   }
   double ldq = 0.0, ldqc = 0.0, res = 0.0, res_c = 0.0;
   int rc_c = 0;
+  PhaseLog plog(st);
   auto run_qc = [&]() {
     if ((rc_c = plan_factor(qc, 1, tau))) return;
+    plog.mark("qc_factor", qc->stream);
     ldqc = qc->logdet;
     cudaMemsetAsync(S.b.p, 0, size_t(n) * r * sizeof(double), qc->stream);
     obs_rhs_kernel<<<int((int64_t(m) * r + 255) / 256), 256, 0, qc->stream>>>(p.d_obs_idx, m, r, tau, y, nullptr,
                                                                                S.b.p);
     if ((rc_c = plan_solve(qc, S.b.p, S.mu.p, r, iters, tol, &res_c))) return;
+    plog.mark("qc_solve", qc->stream);
     if (hutch && (rc_c = plan_solve(qc, V, S.trc.p, nh1, iters, tol, &res_c))) return;
     if (exact && (rc_c = plan_selinv(qc, S.zqc.p))) return;
+    plog.mark("qc_inverse", qc->stream);
   };
   std::thread worker;
   if (qc != &p) {
@@ -677,8 +724,10 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   }
   // Q: log-determinant, then its inverse on the pattern (or Hutchinson solves)
   rc = plan_factor(&p, 0, 0.0);
+  plog.mark("q_factor", st);
   if (!rc) ldq = p.logdet;
   if (!rc && exact) rc = plan_selinv(&p, S.zq.p);
+  plog.mark("q_inverse", st);
   if (!rc && hutch) rc = plan_solve(&p, V, S.trq.p, nh1, iters, tol, &res);
   if (qc != &p) worker.join();
   else if (!rc) run_qc();
@@ -717,6 +766,7 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   obs_trace_kernel<<<nblk, 256, 0, st>>>(p.d_obs_idx, m, exact ? S.zqc.p : nullptr, ns, centre, S.trc.p, V, nh1,
                                          S.part.p);
   const double tr = host_sum_partials(S.part.p, nblk, st);
+  plog.mark("gradient", st);
   p.launches_total += 5 + (hutch ? 1 : 0);  // gbar, adjoint (3), obs trace, probe difference
   API_CUDA(cudaGetLastError());
   const double trace_term = exact ? tr : tr / nh1;

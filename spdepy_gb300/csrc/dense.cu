@@ -639,188 +639,275 @@ __device__ __forceinline__ DF df_fms(DF a, DF b, DF c) {
   err = __fadd_rn(err, __fsub_rn(a.lo, e));
   return df_renorm(s, err);
 }
-// 1 / d: FP32 reciprocal refined by one Newton step with a double-float residual
+// 1 / d: FP32 reciprocal estimate refined by one Newton step with a
+// double-float residual (the step squares the estimate's relative error, so
+// the hardware approximation is enough)
 __device__ __forceinline__ DF df_rcp(DF d) {
-  const float r = __frcp_rn(d.hi);
+  const float r = __fdividef(1.0f, d.hi);
   const DF one_minus = df_fms(DF{1.0f, 0.0f}, d, DF{r, 0.0f});  // 1 - d r
   return df_renorm(r, __fmul_rn(r, one_minus.hi));
 }
 
-// 1 / sqrt(d) rounded to FP32 for a double-float pivot: the FP32 estimate
-// refined by one Newton-Raphson step y (3 - d y^2) / 2 in FP64, which leaves an
-// error far below FP32 rounding (L and L^-1 are stored in FP32).
+// 1 / sqrt(d) rounded to FP32 for a double-float pivot, without the (narrow)
+// FP64 pipe: the hardware estimate y refined by one Newton-Raphson step
+// y + y e / 2 with the residual e = 1 - d y^2 formed from the exact square of y
+// (FMA error terms), which leaves an error far below FP32 rounding.
 __device__ __forceinline__ float df_rsqrt(DF d) {
-  const double x = double(d.hi) + double(d.lo);
-  const double y = rsqrtf(d.hi + d.lo);
-  return float(y * (1.5 - 0.5 * x * y * y));
+  const float y = rsqrtf(d.hi);
+  const float p = __fmul_rn(y, y);
+  const float pe = fmaf(y, y, -p);        // y^2 = p + pe exactly
+  float e = fmaf(-d.hi, p, 1.0f);         // 1 - d_hi p, one rounding
+  e = fmaf(-d.hi, pe, e);
+  e = fmaf(-d.lo, p, e);
+  return fmaf(0.5f * y, e, y);
 }
 
-// The inverse's forward elimination runs one step behind the factorisation in
-// the same barrier interval: step s factors column s (publishing column s + 1),
-// writes the finished column s of L, and eliminates with column s - 1 of L and
-// row s - 1 of L^-1 (publishing row s), so a block takes w + 1 barriers.
+// Blocked double-float factorisation of one diagonal block A = L L^T
+// (w <= 64), in 16-column sub-blocks s with the trailing Schur updates written
+// as A_ik -= (a_ic / d_c) a_kc, so that the pivots d_c and the columns a_ic
+// (at the time column c is eliminated) stay in double-float and L_ic =
+// a_ic / sqrt(d_c) is rounded to FP32 once, at the end.  Per sub-block:
+//   (1) warp 0 eliminates the 16 x 16 diagonal sub-block column by column
+//       (warp-synchronous, each lane holding up to five of its 136 entries);
+//   (2) one thread per row below it eliminates that row's 16 columns and
+//       records S_ic = a_ic / d_c;
+//   (3) the whole CTA applies the rank-16 update S a^T to the trailing lower
+//       triangle, 2 x 2 entries per thread.
+// Then L^-1 (FP32) by sub-blocks: the four 16 x 16 diagonal inverses (one warp
+// each, one lane per column), then the off-diagonal blocks by distance from the
+// diagonal, X_ij = -X_ii (sum_{i > k >= j} L_ik X_kj).  About 20 CTA barriers
+// in all instead of one per column.
+constexpr int kDfSub = 16;
+
+__device__ __forceinline__ int tri_row(int q) {  // largest r with r (r + 1) / 2 <= q
+  int r = int((sqrtf(8.0f * float(q) + 1.0f) - 1.0f) * 0.5f);
+  while (r * (r + 1) / 2 > q) --r;
+  while ((r + 1) * (r + 2) / 2 <= q) ++r;
+  return r;
+}
+
 __global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restrict__ tasks, float* __restrict__ L,
                                                        float* __restrict__ dinv, double* __restrict__ logpiv,
                                                        int* __restrict__ err) {
-  __shared__ float colh[2][kMaxNbk], coll[2][kMaxNbk];
-  __shared__ float dvh[kMaxNbk], dvl[kMaxNbk];
-  __shared__ double dpiv[kMaxNbk];
-  __shared__ float rsq[kMaxNbk];
-  __shared__ float lsh[kMaxNbk][kMaxNbk + 1];
-  __shared__ float xrow[2][kMaxNbk];
+  // Ah/Al: the double-float working matrix (lower triangle); after the
+  // factorisation Al holds L (FP32, zero above the diagonal) and Ah holds L^-1.
+  __shared__ float Ah[kMaxNbk][kMaxNbk + 1], Al[kMaxNbk][kMaxNbk + 1];
+  // S_ic of the current sub-block (double-float); later the inverse's products
+  __shared__ float Sh[kMaxNbk][kDfSub + 1], Sl[kMaxNbk][kDfSub + 1];
+  __shared__ float dph[kMaxNbk], dpl[kMaxNbk], rsq[kMaxNbk];
+  __shared__ float dvh[kDfSub], dvl[kDfSub];
   __shared__ int bad;
   const DiagTask tk = tasks[blockIdx.x];
   const int w = tk.w;
-  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   float* blk = L + tk.a;
-  DF r[4][4];
-#pragma unroll
-  for (int m = 0; m < 4; ++m)
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const int i = ty + 16 * m, k = tx + 16 * n;
-      r[m][n] = DF{(k <= i && i < w) ? blk[int64_t(i) * tk.lda + k] : 0.0f, 0.0f};
-    }
-  float b[4][4];
-#pragma unroll
-  for (int m = 0; m < 4; ++m)
-#pragma unroll
-    for (int n = 0; n < 4; ++n) b[m][n] = (ty + 16 * m == tx + 16 * n) ? 1.0f : 0.0f;
-  if (tid == 0) bad = 0;
-  // publish column 0, its pivot and 1 / L_00; row 0 of L^-1 is (1 / L_00, 0, ...)
-  if (tx == 0) {
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      const int i = ty + 16 * m;
-      if (i < w) { colh[0][i] = r[m][0].hi; coll[0][i] = 0.0f; }
-      if (i == 0) {
-        DF d = r[m][0];
-        if (!(d.hi > 0.0f) || !isfinite(d.hi)) { d = DF{1.0f, 0.0f}; bad = 1; }
-        const DF q = df_rcp(d);
-        dvh[0] = q.hi; dvl[0] = q.lo;
-        dpiv[0] = double(d.hi) + double(d.lo);
-        const float rs = df_rsqrt(d);
-        rsq[0] = rs;
-        b[0][0] = rs;
-        xrow[0][0] = rs;
-      }
+  for (int e = tid; e < w * w; e += 256) {
+    const int i = e / w, k = e - i * w;
+    if (k <= i) {
+      Ah[i][k] = blk[int64_t(i) * tk.lda + k];
+      Al[i][k] = 0.0f;
     }
   }
+  if (tid == 0) bad = 0;
+  // entries of the 16 x 16 lower triangle held by this lane in (1): e = lane + 32 t
+  int eii[5], ekk[5];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    const int e = lane + 32 * t;
+    const int r = tri_row(e < 136 ? e : 0);
+    eii[t] = e < 136 ? r : kDfSub;  // kDfSub: no entry
+    ekk[t] = e < 136 ? e - r * (r + 1) / 2 : 0;
+  }
   __syncthreads();
-  for (int st = 0; st <= w; ++st) {
-    if (st < w) {
-      // ---- factorisation step j = st
-      const int j = st;
-      const float* ch = colh[j & 1];
-      const float* cl = coll[j & 1];
-      const DF dv{dvh[j], dvl[j]};
-      DF ci[4], ck[4];
+  const int nsb = (w + kDfSub - 1) / kDfSub;
+  for (int sb = 0; sb < nsb; ++sb) {
+    const int c0 = sb * kDfSub, cw = min(kDfSub, w - c0);
+    // ---- (1) diagonal sub-block, warp 0; inactive entries are masked, not
+    // branched around, so that the five updates of a lane overlap
+    if (warp == 0) {
+      DF v[5];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int i = ty + 16 * m;
-        ci[m] = (i > j && i < w) ? df_mul(DF{ch[i], cl[i]}, dv) : DF{0.0f, 0.0f};
-      }
+      for (int t = 0; t < 5; ++t)
+        v[t] = eii[t] < cw ? DF{Ah[c0 + eii[t]][c0 + ekk[t]], Al[c0 + eii[t]][c0 + ekk[t]]} : DF{0.0f, 0.0f};
+      for (int j = 0; j < cw; ++j) {
+        // publish column j (its entries are final from here on)
 #pragma unroll
-      for (int n = 0; n < 4; ++n) {
-        const int k = tx + 16 * n;
-        ck[n] = (k > j && k < w) ? DF{ch[k], cl[k]} : DF{0.0f, 0.0f};
-      }
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        if (16 * m + 15 <= j) continue;
-#pragma unroll
-        for (int n = 0; n <= m; ++n) {
-          if (16 * n + 15 <= j) continue;
-          r[m][n] = df_fms(r[m][n], ci[m], ck[n]);
-        }
-      }
-      // column j of L is final: L_ij = a_ij / sqrt(d_j) (threads 0..63 by row)
-      if (tid < w) {
-        const int i = tid;
-        float v = 0.0f;
-        if (i == j) v = 1.0f / rsq[j];
-        else if (i > j) v = (ch[i] + cl[i]) * rsq[j];
-        lsh[i][j] = v;
-      }
-      // publish column j + 1; the owner of its diagonal also publishes the pivot
-      const int jn = j + 1;
-      if (jn < w && tx == (jn & 15)) {
-        const int n = jn >> 4;
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const int i = ty + 16 * m;
-          if (i >= jn && i < w) {
-#pragma unroll
-            for (int nn = 0; nn < 4; ++nn)
-              if (nn == n) {
-                colh[jn & 1][i] = r[m][nn].hi;
-                coll[jn & 1][i] = r[m][nn].lo;
-                if (i == jn) {
-                  DF d = r[m][nn];
-                  if (!(d.hi > 0.0f) || !isfinite(d.hi)) { d = DF{1.0f, 0.0f}; bad = 1; }
-                  const DF q = df_rcp(d);
-                  dvh[jn] = q.hi; dvl[jn] = q.lo;
-                  dpiv[jn] = double(d.hi) + double(d.lo);
-                  rsq[jn] = df_rsqrt(d);
-                }
-              }
+        for (int t = 0; t < 5; ++t)
+          if (eii[t] < cw && ekk[t] == j) {
+            Ah[c0 + eii[t]][c0 + j] = v[t].hi;
+            Al[c0 + eii[t]][c0 + j] = v[t].lo;
           }
+        __syncwarp();
+        DF d{Ah[c0 + j][c0 + j], Al[c0 + j][c0 + j]};
+        const bool nonpos = !(d.hi > 0.0f) || !isfinite(d.hi);
+        if (nonpos) d = DF{1.0f, 0.0f};
+        const DF dv = df_rcp(d);
+        if (lane == 0) {
+          if (nonpos) bad = 1;
+          dph[c0 + j] = d.hi;
+          dpl[c0 + j] = d.lo;
+          dvh[j] = dv.hi;
+          dvl[j] = dv.lo;
         }
-      }
-    }
-    if (st >= 1) {
-      // ---- elimination step j = st - 1 of X = L^-1: B_ic -= L_ij X_jc (i > j, c <= j),
-      // then row j + 1 of X is finished: B_(j+1)c / L_(j+1)(j+1)
-      const int j = st - 1;
-      const float* xr = xrow[j & 1];
-      float li[4], xc[4];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int i = ty + 16 * m;
-        li[m] = (i > j && i < w) ? lsh[i][j] : 0.0f;
-      }
-#pragma unroll
-      for (int n = 0; n < 4; ++n) {
-        const int cc = tx + 16 * n;
-        xc[n] = cc <= j ? xr[cc] : 0.0f;
-      }
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        if (16 * m + 15 <= j) continue;
-#pragma unroll
-        for (int n = 0; n <= m; ++n) {
-          if (16 * n > j) continue;
-          b[m][n] = fmaf(-li[m], xc[n], b[m][n]);
-        }
-      }
-      const int jn = j + 1;
-      if (jn < w && ty == (jn & 15)) {
-        const int m = jn >> 4;
-        const float inv = rsq[jn];
-#pragma unroll
-        for (int mm = 0; mm < 4; ++mm) {
-          if (mm != m) continue;
-#pragma unroll
-          for (int n = 0; n < 4; ++n) {
-            const int cc = tx + 16 * n;
-            if (cc <= jn) {
-              b[mm][n] *= inv;
-              xrow[jn & 1][cc] = b[mm][n];
-            }
-          }
+        for (int t = 0; t < 5; ++t) {
+          const bool act = eii[t] < cw && ekk[t] > j;
+          const int ri = c0 + (act ? eii[t] : j), rk = c0 + (act ? ekk[t] : j);  // (j, j) when masked
+          DF ci = df_mul(DF{Ah[ri][c0 + j], Al[ri][c0 + j]}, dv);
+          DF ck{Ah[rk][c0 + j], Al[rk][c0 + j]};
+          if (!act) ci = ck = DF{0.0f, 0.0f};
+          v[t] = df_fms(v[t], ci, ck);
         }
       }
     }
     __syncthreads();
+    const int b0 = c0 + cw, mt = w - b0;  // rows below the sub-block
+    if (mt <= 0) break;
+    // ---- (2) panel rows, one thread per row; x[0] is the row's entry in
+    // column j, x[c] in column j + c (shifted down after every column, so the
+    // loop over j stays a compact runtime loop)
+    if (tid < mt) {
+      const int i = b0 + tid;
+      DF x[kDfSub];
+#pragma unroll
+      for (int c = 0; c < kDfSub; ++c) x[c] = c < cw ? DF{Ah[i][c0 + c], Al[i][c0 + c]} : DF{0.0f, 0.0f};
+      for (int j = 0; j < cw; ++j) {
+        const DF sj = df_mul(x[0], DF{dvh[j], dvl[j]});
+        Sh[i][j] = sj.hi;
+        Sl[i][j] = sj.lo;
+        Ah[i][c0 + j] = x[0].hi;
+        Al[i][c0 + j] = x[0].lo;
+#pragma unroll
+        for (int c = 1; c < kDfSub; ++c) {
+          const int r = c0 + (j + c < cw ? j + c : j);  // row of the sub-block; unused past its end
+          x[c] = df_fms(x[c], sj, DF{Ah[r][c0 + j], Al[r][c0 + j]});
+        }
+#pragma unroll
+        for (int c = 0; c + 1 < kDfSub; ++c) x[c] = x[c + 1];
+        x[kDfSub - 1] = DF{0.0f, 0.0f};
+      }
+    }
+    __syncthreads();
+    // ---- (3) trailing update A_ik -= sum_c S_ic a_kc, 2 x 2 entries per thread
+    const int nb2 = (mt + 1) >> 1, nq = nb2 * (nb2 + 1) / 2;
+    for (int q = tid; q < nq; q += 256) {
+      const int bi = tri_row(q), bk = q - bi * (bi + 1) / 2;
+      const int i0 = b0 + 2 * bi, k0 = b0 + 2 * bk;
+      const bool i1ok = i0 + 1 < w, k1ok = k0 + 1 < w;
+      DF acc[2][2];
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int i = i0 + r, k = k0 + u;
+          const bool ok = (r == 0 || i1ok) && (u == 0 || k1ok) && k <= i;
+          acc[r][u] = ok ? DF{Ah[i][k], Al[i][k]} : DF{0.0f, 0.0f};
+        }
+      for (int c = 0; c < cw; ++c) {
+        const DF s0{Sh[i0][c], Sl[i0][c]};
+        const DF s1 = i1ok ? DF{Sh[i0 + 1][c], Sl[i0 + 1][c]} : DF{0.0f, 0.0f};
+        const DF a0{Ah[k0][c0 + c], Al[k0][c0 + c]};
+        const DF a1 = k1ok ? DF{Ah[k0 + 1][c0 + c], Al[k0 + 1][c0 + c]} : DF{0.0f, 0.0f};
+        acc[0][0] = df_fms(acc[0][0], s0, a0);
+        acc[1][0] = df_fms(acc[1][0], s1, a0);
+        acc[1][1] = df_fms(acc[1][1], s1, a1);
+        if (bi != bk) acc[0][1] = df_fms(acc[0][1], s0, a1);
+      }
+#pragma unroll
+      for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int i = i0 + r, k = k0 + u;
+          if ((r == 0 || i1ok) && (u == 0 || k1ok) && k <= i) {
+            Ah[i][k] = acc[r][u].hi;
+            Al[i][k] = acc[r][u].lo;
+          }
+        }
+    }
+    __syncthreads();
   }
-  // L (zero above the diagonal) back to the block, row-contiguous
-  for (int e = tid; e < w * w; e += 256) {
-    const int i = e / w, k = e - i * w;
-    blk[int64_t(i) * tk.lda + k] = k <= i ? lsh[i][k] : 0.0f;
+  // ---- L = a_ik / sqrt(d_k) (FP32) into Al and the block: thread (i, q)
+  // holds row i, columns 16 q .. 16 q + 15
+  if (tid < w) rsq[tid] = df_rsqrt(DF{dph[tid], dpl[tid]});
+  __syncthreads();
+  {
+    const int i = tid >> 2, kq = (tid & 3) * kDfSub;
+    float lv[kDfSub];
+#pragma unroll
+    for (int u = 0; u < kDfSub; ++u) {
+      const int k = kq + u;
+      float v = 0.0f;
+      if (i < w && k < w) {
+        if (k < i) v = (Ah[i][k] + Al[i][k]) * rsq[k];
+        else if (k == i) v = 1.0f / rsq[k];
+      }
+      lv[u] = v;
+    }
+    __syncthreads();
+    if (i < w) {
+#pragma unroll
+      for (int u = 0; u < kDfSub; ++u) {
+        const int k = kq + u;
+        if (k < w) {
+          Al[i][k] = lv[u];
+          blk[int64_t(i) * tk.lda + k] = lv[u];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // ---- L^-1 into Ah: diagonal 16 x 16 inverses, warp s, lane = column
+  if (warp < nsb && lane < kDfSub) {
+    const int c0 = warp * kDfSub, cw = min(kDfSub, w - c0), c = lane;
+    if (c < cw) {
+      float x[kDfSub];
+#pragma unroll
+      for (int ii = 0; ii < kDfSub; ++ii) {
+        float v = 0.0f;
+        if (ii == c) v = rsq[c0 + c];
+        else if (ii > c && ii < cw) {
+          float sum = 0.0f;
+#pragma unroll
+          for (int k = 0; k < ii; ++k) sum = fmaf(Al[c0 + ii][c0 + k], x[k], sum);
+          v = -sum * rsq[c0 + ii];
+        }
+        x[ii] = v;
+      }
+#pragma unroll
+      for (int ii = 0; ii < kDfSub; ++ii)
+        if (ii < cw) Ah[c0 + ii][c0 + c] = x[ii];
+    }
+  }
+  __syncthreads();
+  // off-diagonal blocks by distance dd: T = sum_k L_(bi,k) X_(k,bj), then X_(bi,bj) = -X_(bi,bi) T
+  float* Tb = &Sh[0][0];  // up to 3 x 256 products
+  for (int dd = 1; dd < nsb; ++dd) {
+    const int np = nsb - dd;
+    for (int e = tid; e < np * 256; e += 256) {
+      const int pidx = e >> 8, r = (e >> 4) & 15, c = e & 15;
+      const int bi = dd + pidx, bj = pidx;
+      const int i = bi * kDfSub + r;
+      float sum = 0.0f;
+      if (i < w)
+        for (int k = bj * kDfSub; k < bi * kDfSub; ++k) sum = fmaf(Al[i][k], Ah[k][bj * kDfSub + c], sum);
+      Tb[e] = sum;
+    }
+    __syncthreads();
+    for (int e = tid; e < np * 256; e += 256) {
+      const int pidx = e >> 8, r = (e >> 4) & 15, c = e & 15;
+      const int bi = dd + pidx, bj = pidx;
+      const int i = bi * kDfSub + r;
+      if (i < w) {
+        float sum = 0.0f;
+        for (int rr = 0; rr <= r; ++rr) sum = fmaf(Ah[i][bi * kDfSub + rr], Tb[(pidx << 8) + (rr << 4) + c], sum);
+        Ah[i][bj * kDfSub + c] = -sum;
+      }
+    }
+    __syncthreads();
   }
   if (tid < 32) {
     double sum = 0.0;
-    for (int j = tid; j < w; j += 32) sum += 0.5 * log(dpiv[j]);
+    for (int j = tid; j < w; j += 32) sum += 0.5 * log(double(dph[j]) + double(dpl[j]));
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
     if (tid == 0) {
       logpiv[blockIdx.x] = sum;
@@ -828,13 +915,10 @@ __global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restric
     }
   }
   float* dvp = dinv + tk.dinv;
-#pragma unroll
-  for (int m = 0; m < 4; ++m)
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const int i = ty + 16 * m, cc = tx + 16 * n;
-      if (i < w && cc < w) dvp[int64_t(i) * kMaxNbk + cc] = cc <= i ? b[m][n] : 0.0f;
-    }
+  for (int e = tid; e < w * w; e += 256) {
+    const int i = e / w, c = e - i * w;
+    dvp[int64_t(i) * kMaxNbk + c] = c <= i ? Ah[i][c] : 0.0f;
+  }
 }
 
 template <typename T>

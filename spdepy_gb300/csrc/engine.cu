@@ -61,12 +61,14 @@ void Schedule::release() {
 struct Builder {
   Schedule& s;
   int TM, TN;
+  int depth = 0;  // tree depth of the ops begun next
   explicit Builder(Schedule& sc, int tm, int tn) : s(sc), TM(tm), TN(tn) {}
 
   Op& begin(int kind) {
     s.ops.push_back(Op());
     Op& o = s.ops.back();
     o.kind = kind;
+    o.depth = depth;
     switch (kind) {
       case OP_GEMM: o.off = int64_t(s.gemm.size()); break;
       case OP_DIAG: o.off = int64_t(s.diag.size()); break;
@@ -184,6 +186,7 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
   const auto& F = S.fronts;
   for (int d = S.max_depth; d >= 0; --d) {
     const auto& fr = S.by_depth[d];
+    b.depth = d;
     const int pd = d & 1, pc = (d + 1) & 1;
     // zero this depth's update blocks
     int64_t used = 0;
@@ -296,6 +299,7 @@ static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
   const int chunk = std::max(1, std::min(nrhs, 16));
   for (int d = S.max_depth; d >= 0; --d) {
     const auto& fr = S.by_depth[d];
+    b.depth = d;
     const int pd = d & 1;
     Op& og = b.begin(OP_SGATHER_FWD);
     og.depth = d;
@@ -351,6 +355,7 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
   const int chunk = std::max(1, std::min(nrhs, 16));
   for (int d = 0; d <= S.max_depth; ++d) {
     const auto& fr = S.by_depth[d];
+    b.depth = d;
     const int pd = d & 1;
     Op& og = b.begin(OP_SGATHER_BWD);
     og.depth = d;
@@ -417,6 +422,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
   int64_t scratch = 32;
   for (int d = 0; d <= S.max_depth; ++d) {
     const auto& fr = S.by_depth[d];
+    b.depth = d;
     const int pz = (d & 1) ? B_P1 : B_P0;
     // scratch layout of this depth: W, W^T, X^T, TT per front
     struct Sx { int64_t w, wt, xt, tt; int ldw, ldx; std::vector<std::vector<std::array<int, 3>>> levels; };
@@ -843,7 +849,17 @@ struct Exec {
   }
   void run() {
     cudaStream_t st = p->stream;
+    // optional per-depth timeline (SPDE_PHASE_LOG): an event at every change of depth
+    static const bool depth_log = std::getenv("SPDE_PHASE_LOG") != nullptr;
+    std::vector<std::pair<int, cudaEvent_t>> dmarks;
+    auto dmark = [&](int d) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      cudaEventRecord(e, st);
+      dmarks.emplace_back(d, e);
+    };
     for (const Op& o : s.ops) {
+      if (depth_log && (dmarks.empty() || dmarks.back().first != o.depth)) dmark(o.depth);
       const bool on_tc = o.kind == OP_GEMM && sizeof(T) == sizeof(float) && o.tc == kPathTensor && tc_gemm_enabled();
       const bool timed = p->profile && o.kind != OP_MEMSET && (on_tc || !p->profile_tc_only);
       if (timed) prof_begin(p, st);
@@ -888,6 +904,21 @@ struct Exec {
           break;
       }
       if (timed) prof_end(p, st, on_tc ? kProfTensorCore : o.kind, o.flops, o.site, o.kind == OP_GEMM ? o.count : 0);
+    }
+    if (depth_log && !dmarks.empty()) {
+      dmark(-1);
+      const char* what = &s == &p->sched_factor ? "factor" : &s == &p->sched_selinv ? "inverse" : "solve";
+      std::string line = std::string(what) + " ms by depth:";
+      for (size_t i = 0; i + 1 < dmarks.size(); ++i) {
+        float ms = 0.0f;
+        cudaEventSynchronize(dmarks[i + 1].second);
+        cudaEventElapsedTime(&ms, dmarks[i].second, dmarks[i + 1].second);
+        char buf[48];
+        std::snprintf(buf, sizeof(buf), " %d:%.2f", dmarks[i].first, ms);
+        line += buf;
+      }
+      for (auto& m : dmarks) cudaEventDestroy(m.second);
+      std::fprintf(stderr, "%s\n", line.c_str());
     }
     p->launches_total += s.launches;
   }
