@@ -763,28 +763,42 @@ __global__ void __launch_bounds__(256) potrf_df_kernel(const DiagTask* __restric
     __syncthreads();
     const int b0 = c0 + cw, mt = w - b0;  // rows below the sub-block
     if (mt <= 0) break;
-    // ---- (2) panel rows, one thread per row; x[0] is the row's entry in
-    // column j, x[c] in column j + c (shifted down after every column, so the
-    // loop over j stays a compact runtime loop)
-    if (tid < mt) {
-      const int i = b0 + tid;
-      DF x[kDfSub];
+    // ---- (2) panel rows, four threads per row: thread q holds the row's
+    // entries in columns q, q + 4, q + 8, q + 12 of the sub-block; the owner of
+    // column j forms S_ij and passes it to the other three by shuffle
+    const unsigned pmask = __ballot_sync(0xffffffffu, tid < 4 * mt);
+    if (tid < 4 * mt) {
+      const int i = b0 + (tid >> 2), q = tid & 3;
+      DF x[4];
 #pragma unroll
-      for (int c = 0; c < kDfSub; ++c) x[c] = c < cw ? DF{Ah[i][c0 + c], Al[i][c0 + c]} : DF{0.0f, 0.0f};
+      for (int u = 0; u < 4; ++u) {
+        const int c = q + 4 * u;
+        x[u] = c < cw ? DF{Ah[i][c0 + c], Al[i][c0 + c]} : DF{0.0f, 0.0f};
+      }
       for (int j = 0; j < cw; ++j) {
-        const DF sj = df_mul(x[0], DF{dvh[j], dvl[j]});
-        Sh[i][j] = sj.hi;
-        Sl[i][j] = sj.lo;
-        Ah[i][c0 + j] = x[0].hi;
-        Al[i][c0 + j] = x[0].lo;
-#pragma unroll
-        for (int c = 1; c < kDfSub; ++c) {
-          const int r = c0 + (j + c < cw ? j + c : j);  // row of the sub-block; unused past its end
-          x[c] = df_fms(x[c], sj, DF{Ah[r][c0 + j], Al[r][c0 + j]});
+        const int uj = j >> 2, qj = j & 3;
+        DF xj = x[0];
+        if (uj == 1) xj = x[1];
+        if (uj == 2) xj = x[2];
+        if (uj == 3) xj = x[3];
+        DF sj = df_mul(xj, DF{dvh[j], dvl[j]});
+        const int src = (lane & ~3) | qj;
+        sj.hi = __shfl_sync(pmask, sj.hi, src);
+        sj.lo = __shfl_sync(pmask, sj.lo, src);
+        if (q == qj) {
+          Sh[i][j] = sj.hi;
+          Sl[i][j] = sj.lo;
+          Ah[i][c0 + j] = xj.hi;
+          Al[i][c0 + j] = xj.lo;
         }
 #pragma unroll
-        for (int c = 0; c + 1 < kDfSub; ++c) x[c] = x[c + 1];
-        x[kDfSub - 1] = DF{0.0f, 0.0f};
+        for (int u = 0; u < 4; ++u) {
+          const int c = q + 4 * u;
+          const bool act = c > j && c < cw;
+          const int r = c0 + (act ? c : j);  // (j, j) when masked
+          const DF nx = df_fms(x[u], sj, DF{Ah[r][c0 + j], Al[r][c0 + j]});
+          if (act) x[u] = nx;
+        }
       }
     }
     __syncthreads();
