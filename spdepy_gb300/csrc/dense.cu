@@ -669,8 +669,8 @@ __device__ __forceinline__ float df_rsqrt(DF d) {
 // a_ic / sqrt(d_c) is rounded to FP32 once, at the end.  Per sub-block:
 //   (1) warp 0 eliminates the 16 x 16 diagonal sub-block column by column
 //       (warp-synchronous, each lane holding up to five of its 136 entries);
-//   (2) one thread per row below it eliminates that row's 16 columns and
-//       records S_ic = a_ic / d_c;
+//   (2) four threads per row below it eliminate that row's 16 columns and
+//       record S_ic = a_ic / d_c;
 //   (3) the whole CTA applies the rank-16 update S a^T to the trailing lower
 //       triangle, 2 x 2 entries per thread.
 // Then L^-1 (FP32) by sub-blocks: the four 16 x 16 diagonal inverses (one warp
