@@ -118,9 +118,9 @@ __global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const int* 
 // weights offset-major (w[o n + p]), so every offset's read is coalesced.  The
 // 27 offsets are unrolled (compile-time displacements, loads issued together);
 // node indices fit in 32 bits (checked by the caller).
-template <int TRANS>
-__global__ void pc_apply_kernel(QStencil q, const float* __restrict__ w, const double* __restrict__ x,
-                                double* __restrict__ out, int nrhs) {
+template <int TRANS, typename TIn, typename TOut>
+__global__ void pc_apply_kernel(QStencil q, const float* __restrict__ w, const TIn* __restrict__ x,
+                                TOut* __restrict__ out, int nrhs) {
   const int n = q.Ns * q.T;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n * nrhs) return;
@@ -142,7 +142,15 @@ __global__ void pc_apply_kernel(QStencil q, const float* __restrict__ w, const d
     const float wv = TRANS ? w[int64_t(o) * n + nb] : w[int64_t(o) * n + p];
     acc = fmaf(wv, float(x[int64_t(nb) * nrhs + r]), acc);
   }
-  out[e] = double(acc);
+  out[e] = TOut(acc);
+}
+
+// FP32 copy of a vector: the preconditioner reads every entry from 27 nodes,
+// so converting once here keeps FP64 -> FP32 conversions (on the narrow FP64
+// pipe of this part) out of the stencil passes.
+__global__ void pc_to_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t len) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < len) y[i] = float(x[i]);
 }
 
 // Jacobi: out = x / A_pp
@@ -398,8 +406,12 @@ void apply_precond(Plan* p, int kind, const float* w, const int* obs, double tau
   } else if (kind == 1) {
     pc_jacobi_kernel<<<nblk(len), 256, 0, p->stream>>>(q, obs, tau, r, z, nrhs);
   } else {
-    pc_apply_kernel<0><<<nblk(len), 256, 0, p->stream>>>(q, w, r, tmp, nrhs);
-    pc_apply_kernel<1><<<nblk(len), 256, 0, p->stream>>>(q, w, tmp, z, nrhs);
+    // FP32 copy of r and the FP32 intermediate G r share tmp (len doubles)
+    float* r32 = reinterpret_cast<float*>(tmp);
+    float* t32 = r32 + len;
+    pc_to_f32_kernel<<<nblk(len), 256, 0, p->stream>>>(r, r32, len);
+    pc_apply_kernel<0, float, float><<<nblk(len), 256, 0, p->stream>>>(q, w, r32, t32, nrhs);
+    pc_apply_kernel<1, float, double><<<nblk(len), 256, 0, p->stream>>>(q, w, t32, z, nrhs);
   }
 }
 
@@ -500,11 +512,11 @@ int pc_grad(Plan* p, int with_obs, double tau, const float* prm, const float* w,
   const QStencil q = p->qstencil();
   const int* obs = with_obs ? p->d_obs_cnt : nullptr;
   cudaStream_t st = p->stream;
-  pc_apply_kernel<1><<<nblk(len), 256, 0, st>>>(q, w, z, y, k);           // y = G^T z
+  pc_apply_kernel<1, double, double><<<nblk(len), 256, 0, st>>>(q, w, z, y, k);           // y = G^T z
   launch_spmv(q, obs, tau, y, u, k, st);                                   // u = A y
-  pc_apply_kernel<0><<<nblk(len), 256, 0, st>>>(q, w, u, e, k);           // v = G u
+  pc_apply_kernel<0, double, double><<<nblk(len), 256, 0, st>>>(q, w, u, e, k);           // v = G u
   pc_sub_kernel<<<nblk(len), 256, 0, st>>>(z, e, len);                     // e = z - v
-  pc_apply_kernel<1><<<nblk(len), 256, 0, st>>>(q, w, e, g1, k);          // G^T e
+  pc_apply_kernel<1, double, double><<<nblk(len), 256, 0, st>>>(q, w, e, g1, k);          // G^T e
   launch_spmv(q, obs, tau, g1, g2, k, st);                                 // g = A G^T e
   // loss = ||e||^2 / (n k): one column of length n k
   pc_dot_partial_kernel<<<kDotBlocks, 256, 0, st>>>(e, e, len, 1, part);
