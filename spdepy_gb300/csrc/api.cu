@@ -547,6 +547,7 @@ int spde_spmv(SpdePlan* plan, int with_obs, double tau, const double* x, double*
   if (!plan || !x || !y || nrhs < 1) return SPDE_ERR_ARG;
   Plan& p = plan->p;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   launch_spmv(p.qstencil(), with_obs ? p.d_obs_cnt : nullptr, tau, x, y, nrhs, p.stream);
   API_CUDA(cudaGetLastError());
   return SPDE_OK;
@@ -603,14 +604,12 @@ int spde_adjoint(SpdePlan* plan, const double* gbar, double* grad_host) {
   Plan& p = plan->p;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   const int nt = ntheta_of(p) - 1;
-  double *work = nullptr, *g = nullptr;
-  API_CUDA(cudaMalloc(&work, size_t(adjoint_work_elems(&p)) * sizeof(double)));
-  API_CUDA(cudaMalloc(&g, size_t(nt) * sizeof(double)));
-  launch_adjoint(&p, gbar, g, work, p.stream);
-  cudaError_t e = cudaMemcpyAsync(grad_host, g, nt * sizeof(double), cudaMemcpyDeviceToHost, p.stream);
+  DevBuf work, g;  // freed on every return
+  API_CUDA(work.ensure(size_t(adjoint_work_elems(&p))));
+  API_CUDA(g.ensure(size_t(nt)));
+  launch_adjoint(&p, gbar, g.p, work.p, p.stream);
+  cudaError_t e = cudaMemcpyAsync(grad_host, g.p, nt * sizeof(double), cudaMemcpyDeviceToHost, p.stream);
   cudaStreamSynchronize(p.stream);
-  cudaFree(work);
-  cudaFree(g);
   if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) { p.last_error = "adjoint failed"; return SPDE_ERR_CUDA; }
   return SPDE_OK;
 }
@@ -643,8 +642,9 @@ int spde_conditional_mean(SpdePlan* plan, double tau, const double* y, const dou
   if (!p.d_obs_idx) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   int rc = plan_factor(&p, 1, tau);
   if (rc) return rc;
-  double* b = nullptr;
-  API_CUDA(cudaMalloc(&b, size_t(p.sym.n) * sizeof(double)));
+  DevBuf buf;  // right-hand side; freed on every return
+  API_CUDA(buf.ensure(size_t(p.sym.n)));
+  double* b = buf.p;
   API_CUDA(cudaMemsetAsync(b, 0, size_t(p.sym.n) * sizeof(double), p.stream));
   obs_rhs_kernel<<<(p.nobs + 255) / 256 + 1, 256, 0, p.stream>>>(p.d_obs_idx, p.nobs, 1, tau, y, mu0, b);
   double resid = 0.0;
@@ -655,8 +655,7 @@ int spde_conditional_mean(SpdePlan* plan, double tau, const double* y, const dou
     sub_kernel<<<int((p.sym.n + 255) / 256), 256, 0, p.stream>>>(b, mu0, p.sym.n);
     sub_kernel<<<int((p.sym.n + 255) / 256), 256, 0, p.stream>>>(mu, b, p.sym.n);
   }
-  cudaStreamSynchronize(p.stream);
-  cudaFree(b);
+  cudaStreamSynchronize(p.stream);  // before buf is freed
   return rc;
 }
 
@@ -835,7 +834,7 @@ int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, i
 
 int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, const double* V, int nh1, int precond,
                           const float* w_q, const float* w_qc, double tol, int maxit, double* jac, int* iters) {
-  if (!plan || !y || r < 1 || !V || nh1 < 1 || !jac || precond < 0 || precond > 2 ||
+  if (!plan || !y || r < 1 || !V || nh1 < 1 || !jac || maxit < 1 || precond < 0 || precond > 2 ||
       (precond == 2 && (!w_q || !w_qc)))
     return SPDE_ERR_ARG;
   Plan& p = plan->p;
