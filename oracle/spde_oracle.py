@@ -12,6 +12,7 @@ Reference files followed (paths inside the reference project):
   grids/spatial2D_regular_mesh.py                                spatial Grid
   spdes/whittle_matern*2D.py, spdes/var_whittle_matern*2D.py      spatial models
   spdes/{,var_,cov_}advection_{,var_}{,i,ha_}diffusion2D.py       spatio-temporal models
+  spdes/seperable_spatial_temporal{,_idiffusion}2D.py              separable space-time models
   model.py:73-87,120-127                                          sample / update
 
 Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
@@ -642,6 +643,94 @@ class OracleModel:
         Q = self.makeQ(par)
         Qc = (Q + (S.T @ S) * tau).tocsc()
         return self.factor(Qc).solve(S.T @ np.asarray(y, float) * tau)
+
+
+class SeparableOracleModel(OracleModel):
+    """Separable space-time model Q = Qt (x) Qs, restated on CPU (FP64).
+
+    Qs is the spatially varying Whittle-Matern precision A^T V^-1 A with
+    A = V kappa - A_H(H) (the var-Whittle-Matern spatial part,
+    spdes/var_whittle_matern_anisotropic2D.py:66-82), with B-spline fields for
+    kappa, gamma and, for the anisotropic form, vx and vy (H = gamma I + v v^T per
+    face; the isotropic form has H = gamma I).  Qt is a tridiagonal AR(1)
+    precision over the T time steps, in one of two parametrisations:
+
+    * ``temporal="rho"`` (spdes/seperable_spatial_temporal2D.py:64-83,186-212):
+      rho = exp(par[ns]), Qt_tt = 1 / (1 - rho^2) at both ends and
+      (1 + rho^2) / (1 - rho^2) inside, Qt_t,t+1 = -rho / (1 - rho^2);
+      parameters kappa, gamma, vx, vy, log rho, log tau.
+    * ``temporal="a-sigma"`` (spdes/seperable_spatial_temporal_idiffusion2D.py:
+      63-103,166-189): a = par[ns], sigma = exp(par[ns + 1]), Qt_tt = sigma at both
+      ends and (1 + a^2) sigma inside, Qt_t,t+1 = -a sigma; parameters kappa,
+      gamma, a, log sigma, log tau.  The reference fills Qt in a loop over
+      range(10), so its class only works for T = 10; this restatement follows the
+      evident formula for any T.
+
+    dQ follows the reference's order: every spatial parameter as Qt (x) dQs_i,
+    then the temporal ones (Qt' (x) Qs, and Q itself for log sigma).
+    """
+
+    def __init__(self, grid: OracleGrid, diff, bc, temporal="rho"):
+        if temporal not in ("rho", "a-sigma"):
+            raise ValueError(f"unknown temporal parametrisation {temporal}")
+        if grid.T < 2:
+            raise ValueError("a separable space-time model needs T >= 2")
+        self.grid = grid
+        self.fam = Family("var-whittle-matern", diff, grid.Nbs2)  # the spatial parameter layout
+        self.bc = bc
+        self.ww = None
+        self.derivative = "reference"
+        self.temporal = temporal
+        self.ns = self.fam.nself  # spatial parameters, before the temporal ones
+
+    def _spatial(self, par):
+        """The spatial parameters in the var-Whittle-Matern layout (tau last, unused by Qs)."""
+        par = np.asarray(par, float)
+        return np.hstack([par[:self.ns], par[-1]])
+
+    def qt(self, par, deriv=False):
+        """Qt, or its derivative in the first temporal parameter (log rho, or a)."""
+        T = self.grid.T
+        par = np.asarray(par, float)
+        main = np.empty(T)
+        if self.temporal == "rho":
+            rho = np.exp(par[self.ns])
+            q = 1.0 - rho * rho
+            if deriv:  # rho d/drho
+                main[:] = 4.0 * rho * rho / (q * q)
+                main[[0, -1]] = 2.0 * rho * rho / (q * q)
+                off = -rho * (1.0 + rho * rho) / (q * q)
+            else:
+                main[:] = (1.0 + rho * rho) / q
+                main[[0, -1]] = 1.0 / q
+                off = -rho / q
+        else:
+            a, sigma = par[self.ns], np.exp(par[self.ns + 1])
+            if deriv:  # d/da
+                main[:] = 2.0 * a * sigma
+                main[[0, -1]] = 0.0
+                off = -sigma
+            else:
+                main[:] = (1.0 + a * a) * sigma
+                main[[0, -1]] = sigma
+                off = -a * sigma
+        return sparse.diags([np.full(T - 1, off), main, np.full(T - 1, off)], [-1, 0, 1], format="csc")
+
+    def makeQ(self, par):
+        Qs = self._wm_Q(self.fam, self._spatial(par))[0]
+        return sparse.kron(self.qt(par), Qs, format="csc")
+
+    def dQ_list(self, par):
+        g = self.grid
+        spar = self._spatial(par)
+        Qs, A, _, _ = self._wm_Q(self.fam, spar)
+        Qt = self.qt(par)
+        out = [sparse.kron(Qt, ((dA.T @ A + A.T @ dA) / g.V).tocsc(), format="csc")
+               for _, dA, _ in self._dA_list(spar)]
+        out.append(sparse.kron(self.qt(par, deriv=True), Qs, format="csc"))
+        if self.temporal == "a-sigma":
+            out.append(sparse.kron(Qt, Qs, format="csc"))  # d/dlog sigma: Q is linear in sigma
+        return out
 
 
 class DenseOrSparseFactor:

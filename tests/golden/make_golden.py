@@ -17,6 +17,12 @@ the CUDA path.  Cases:
   ``logLike(par, nh1, grad=True)`` with ``np.random.seed`` fixed before the call
   (reference e.g. ``spdes/advection_diffusion2D.py:187-223``).
 * ``facade_wm``  ``Model.update`` conditional mean (reference ``model.py:120-127``).
+* ``separable_*`` separable space-time models Q = Qt (x) Qs, as the ``model_*``
+  cases (reference ``spdes/seperable_spatial_temporal2D.py`` and
+  ``seperable_spatial_temporal_idiffusion2D.py``).  They pin the oracle only; the
+  CUDA path does not cover this family yet, so they carry their own prefix.
+
+``python tests/golden/make_golden.py --only separable`` regenerates just those.
 """
 from __future__ import annotations
 
@@ -112,7 +118,7 @@ def _simulate(Q, S, noise_sd, seed):
     return S @ x + noise_sd * rng.normal(size=S.shape[0])
 
 
-def _model_case(name, mod, par, idx, noise_sd, gridinfo, extra=None):
+def _model_case(name, mod, par, idx, noise_sd, gridinfo, extra=None, prefix="model"):
     Q = mod.Q if mod.Q is not None else mod.makeQ(par, grad=False)[0]
     S = mod.grid.getS(idx)
     y = _simulate(Q, S, noise_sd, seed=11)
@@ -124,7 +130,7 @@ def _model_case(name, mod, par, idx, noise_sd, gridinfo, extra=None):
                nh1=NH1, seed_v=SEED_V, **_csr(Q), **gridinfo)
     if extra:
         rec.update(extra)
-    np.savez_compressed(os.path.join(OUT, f"model_{name}.npz"), **rec)
+    np.savez_compressed(os.path.join(OUT, f"{prefix}_{name}.npz"), **rec)
     print(f"{name}: n={Q.shape[0]} nnz={Q.nnz} f={f:.12g} |jac|={np.linalg.norm(jac):.6g}")
 
 
@@ -262,5 +268,38 @@ def main():
     print("facade_wm: mu norm", np.linalg.norm(model.mu))
 
 
+def separable_cases(sp=None):
+    """Separable space-time fixtures: the rho form (anisotropic, bc 1 and 3) and
+    the (a, sigma) form (isotropic; the reference class needs T = 10)."""
+    sp = sp or ref_harness.load_reference()
+    from spdepy.spdes.seperable_spatial_temporal2D import SeperableSpatialTemporal2D
+    from spdepy.spdes.seperable_spatial_temporal_idiffusion2D import SeperableSpatialTemporalIDiffusion2D
+    for bc in (1, 3):
+        M, N, T = 10, 9, 5
+        g, gi = _st_grid(sp, M, N, T)
+        rng = np.random.default_rng(50 + bc)
+        par = np.hstack([np.log(0.5) + 0.1 * rng.normal(size=9), np.log(0.6) + 0.1 * rng.normal(size=9),
+                         0.3 * rng.normal(size=9), 0.3 * rng.normal(size=9), np.log(0.6), np.log(100.0)])
+        mod = SeperableSpatialTemporal2D(grid=g, par=par, bc=bc)
+        idx = np.random.default_rng(53 + bc).choice(M * N * T, 120, replace=False)
+        _model_case(f"ani_bc{bc}", mod, par, idx, 0.1,
+                    dict(gi, bc=bc, family="seperable-spatial-temporal", ani=1, ha=0, temporal="rho"),
+                    prefix="separable")
+    M, N, T = 8, 7, 10
+    g, gi = _st_grid(sp, M, N, T)
+    rng = np.random.default_rng(57)
+    par = np.hstack([np.log(0.5) + 0.1 * rng.normal(size=9), np.log(0.6) + 0.1 * rng.normal(size=9), 0.5,
+                     np.log(2.0), np.log(100.0)])
+    mod = SeperableSpatialTemporalIDiffusion2D(grid=g, par=par, bc=3)
+    idx = np.random.default_rng(58).choice(M * N * T, 110, replace=False)
+    _model_case("iso_bc3", mod, par, idx, 0.1,
+                dict(gi, bc=3, family="seperable-spatial-temporal", ani=0, ha=0, temporal="a-sigma"),
+                prefix="separable")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "separable":
+        separable_cases()
+    else:
+        main()
+        separable_cases()

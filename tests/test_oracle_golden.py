@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 from scipy import sparse
 
-from golden_cases import load, model_cases, oracle_model
+from golden_cases import load, model_cases, oracle_model, separable_cases, separable_oracle
 from oracle import stencils as S
 
 
@@ -39,6 +39,41 @@ def test_model_golden(name):
     assert abs(f - float(g["f"])) <= 1e-12 * abs(float(g["f"]))
     fg, jac = mod.loglike(par, g["y"], g["idx"], grad=True, nh1=int(g["nh1"]), seed=int(g["seed_v"]))
     assert np.allclose(jac, g["jac"], rtol=1e-10, atol=1e-12 * np.abs(g["jac"]).max())
+
+
+@pytest.mark.parametrize("name", separable_cases())
+def test_separable_golden(name):
+    """Q = Qt (x) Qs, the objective and the Hutchinson gradient of the reference's
+    separable space-time classes."""
+    g = load(name)
+    mod = separable_oracle(g)
+    par = g["par"]
+    Q = mod.makeQ(par)
+    Qg = sparse.csr_matrix((g["Q_data"], g["Q_indices"], g["Q_indptr"]), shape=Q.shape)
+    assert abs(Q - Qg).max() <= 1e-13 * abs(Qg).max()
+    assert len(mod.dQ_list(par)) == par.size - 1
+    f = mod.loglike(par, g["y"], g["idx"], grad=False)
+    assert abs(f - float(g["f"])) <= 1e-12 * abs(float(g["f"]))
+    fg, jac = mod.loglike(par, g["y"], g["idx"], grad=True, nh1=int(g["nh1"]), seed=int(g["seed_v"]))
+    assert np.allclose(jac, g["jac"], rtol=1e-10, atol=1e-12 * np.abs(g["jac"]).max())
+
+
+def test_separable_derivatives_by_differences():
+    """The analytic dQ list of the separable oracle against central differences of
+    its own Q (this also checks the temporal derivatives, which the golden
+    Hutchinson gradient only sees through a random projection)."""
+    for name in separable_cases():
+        g = load(name)
+        mod = separable_oracle(g)
+        par = np.asarray(g["par"], float)
+        dQ = mod.dQ_list(par)
+        for i in range(par.size - 1):
+            h = 1e-6 * max(1.0, abs(par[i]))
+            pp, pm = par.copy(), par.copy()
+            pp[i] += h
+            pm[i] -= h
+            fd = (mod.makeQ(pp) - mod.makeQ(pm)) / (2 * h)
+            assert abs(fd - dQ[i]).max() <= 1e-6 * max(abs(dQ[i]).max(), 1e-8), (name, i)
 
 
 def test_facade_update_golden():
