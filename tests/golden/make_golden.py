@@ -22,7 +22,7 @@ the CUDA path.  Cases:
   ``seperable_spatial_temporal_idiffusion2D.py``).  They pin the oracle only; the
   CUDA path does not cover this family yet, so they carry their own prefix.
 
-``python tests/golden/make_golden.py --only separable`` regenerates just those.
+``python tests/golden/make_golden.py --only separable [name ...]`` regenerates just those.
 """
 from __future__ import annotations
 
@@ -268,13 +268,18 @@ def main():
     print("facade_wm: mu norm", np.linalg.norm(model.mu))
 
 
-def separable_cases(sp=None):
+def separable_cases(sp=None, only=None):
     """Separable space-time fixtures: the rho form (anisotropic, bc 1 and 3) and
-    the (a, sigma) form (isotropic; the reference class needs T = 10)."""
+    the (a, sigma) form (isotropic and half-angle; those reference classes need
+    T = 10).  `only`: names to (re)generate, all when None."""
     sp = sp or ref_harness.load_reference()
     from spdepy.spdes.seperable_spatial_temporal2D import SeperableSpatialTemporal2D
+    from spdepy.spdes.seperable_spatial_temporal_ha2D import SeperableSpatialTemporalHa2D
     from spdepy.spdes.seperable_spatial_temporal_idiffusion2D import SeperableSpatialTemporalIDiffusion2D
+    want = (lambda name: only is None or name in only)
     for bc in (1, 3):
+        if not want(f"ani_bc{bc}"):
+            continue
         M, N, T = 10, 9, 5
         g, gi = _st_grid(sp, M, N, T)
         rng = np.random.default_rng(50 + bc)
@@ -285,6 +290,19 @@ def separable_cases(sp=None):
         _model_case(f"ani_bc{bc}", mod, par, idx, 0.1,
                     dict(gi, bc=bc, family="seperable-spatial-temporal", ani=1, ha=0, temporal="rho"),
                     prefix="separable")
+    if want("ha_bc1"):
+        M, N, T = 8, 7, 10
+        g, gi = _st_grid(sp, M, N, T)
+        rng = np.random.default_rng(59)
+        par = np.hstack([np.log(0.5) + 0.1 * rng.normal(size=9), np.log(0.6) + 0.1 * rng.normal(size=9),
+                         0.3 * rng.normal(size=9), 0.3 * rng.normal(size=9), 0.4, np.log(1.5), np.log(100.0)])
+        mod = SeperableSpatialTemporalHa2D(grid=g, par=par, bc=1)
+        idx = np.random.default_rng(60).choice(M * N * T, 110, replace=False)
+        _model_case("ha_bc1", mod, par, idx, 0.1,
+                    dict(gi, bc=1, family="seperable-spatial-temporal", ani=1, ha=1, temporal="a-sigma"),
+                    prefix="separable")
+    if not want("iso_bc3"):
+        return
     M, N, T = 8, 7, 10
     g, gi = _st_grid(sp, M, N, T)
     rng = np.random.default_rng(57)
@@ -299,7 +317,7 @@ def separable_cases(sp=None):
 
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "separable":
-        separable_cases()
+        separable_cases(only=sys.argv[3:] or None)
     else:
         main()
         separable_cases()
