@@ -59,3 +59,17 @@ def test_reference_arm_is_rank0_only(capsys):
         gpus, steps, warmup = 2, 1, 1
     bench.run_reference(A(), rank=1, world=2)
     assert capsys.readouterr().out == ""
+
+
+def test_cpu_figures_scale_to_the_workload():
+    """The CPU baseline scales the largest sampled sub-grid linearly in nodes to
+    the benchmarked workload and reports the fitted cost exponent beside it."""
+    sys.path.insert(0, ROOT)
+    import bench
+    # cost ~ n^2: 1 s at 1,000 nodes, 4 s at 2,000 nodes
+    cb = bench._cpu_figures([(1000, 1.0), (2000, 4.0)], n_full=20000, passes=1)
+    assert cb["cost_exponent"] == pytest.approx(2.0)
+    assert cb["value"] == pytest.approx(1.0 / (4.0 * 10.0))          # linear in nodes from the largest sample
+    assert cb["value_power_law"] == pytest.approx(1.0 / (4.0 * 100.0))
+    assert cb["sample_evals_per_s"] == pytest.approx(0.25) and cb["sample_nodes"] == 2000
+    assert cb["unit"] == "evals/s" and cb["kind"] == "port"
