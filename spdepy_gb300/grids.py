@@ -65,6 +65,10 @@ class Grid:
             self.px, self.py = sxe.ravel(), sye.ravel()
         else:
             self.px, self.py = self.sx, self.sy
+        # covariate / intercept columns of S (reference addCov / addInt)
+        self.cov = None
+        self.inter = False
+        self.scale = False
         self.bs = self._basis(self.px, self.py, (0.0, 0.0))
         shifts = {0: (-self.hx / 2, 0.0), 1: (self.hx / 2, 0.0), 2: (0.0, -self.hy / 2), 3: (0.0, self.hy / 2)}
         self.bsH = np.stack([self._basis(self.px, self.py, shifts[f]) for f in range(4)], axis=1)
@@ -159,10 +163,42 @@ class Grid:
         return self.n2e(idx)
 
     def getS(self, idxs=None):
-        """Observation matrix S (selected identity rows, reference :35-58)."""
+        """Observation matrix S (reference :35-58): selected identity rows over the
+        lattice nodes, followed by the fixed-effect columns when set, in the
+        reference's order: [1, cov] (cov / max(cov) with scale) after addCov with
+        an intercept, [cov] without one, [1] after addInt alone."""
         cols = self.obs_nodes(idxs)
         m = cols.size
-        return sparse.csc_matrix((np.ones(m), (np.arange(m), cols)), shape=(m, self.n))
+        S = sparse.csc_matrix((np.ones(m), (np.arange(m), cols)), shape=(m, self.n))
+        extra = self._fixed_effects()
+        if extra is None:
+            return S
+        rows = np.arange(self.M * self.N * self.T) if idxs is None else np.asarray(idxs, dtype=np.int64)
+        return sparse.hstack([S, sparse.csc_matrix(extra[rows])], format="csc")
+
+    def _fixed_effects(self):
+        """Dense fixed-effect columns over all M N T observation positions, or None."""
+        npos = self.M * self.N * self.T
+        if self.cov is not None:
+            cov = np.asarray(self.cov, dtype=np.float64).reshape(-1)
+            if cov.size != npos:
+                raise ValueError(f"covariate has {cov.size} values, the grid {npos} observation positions")
+            if self.inter:
+                return np.stack([np.ones(npos), cov / cov.max() if self.scale else cov], axis=1)
+            return cov.reshape(-1, 1)
+        if self.inter:
+            return np.ones((npos, 1))
+        return None
+
+    def addCov(self, cov, inter=True, scale=False):
+        """Covariate (and intercept) columns of S (reference :60-64)."""
+        self.inter = inter
+        self.scale = scale
+        self.cov = np.asarray(cov, dtype=np.float64)
+
+    def addInt(self):
+        """Intercept column of S (reference :66-68)."""
+        self.inter = True
 
     def spatial(self):
         """The spatial grid of the initial-field model."""

@@ -22,7 +22,12 @@ the CUDA path.  Cases:
   ``seperable_spatial_temporal_idiffusion2D.py``).  They pin the oracle only; the
   CUDA path does not cover this family yet, so they carry their own prefix.
 
-``python tests/golden/make_golden.py --only separable [name ...]`` regenerates just those.
+* ``grid_getS``  the observation matrix with fixed-effect columns: ``Grid.getS``
+  after ``addInt`` / ``addCov`` (with and without intercept and scaling) on a
+  padded space-time grid (reference ``grids/spat2Dtemp_regular_mesh.py:35-68``).
+
+``python tests/golden/make_golden.py --only separable [name ...]`` regenerates just
+the separable cases, ``--only getS`` the grid_getS fixture.
 """
 from __future__ import annotations
 
@@ -268,6 +273,34 @@ def main():
     print("facade_wm: mu norm", np.linalg.norm(model.mu))
 
 
+def getS_cases(sp=None):
+    """Grid.getS with fixed-effect columns on a padded space-time grid."""
+    sp = sp or ref_harness.load_reference()
+    M, N, T, ext = 6, 5, 3, 1
+    rng = np.random.default_rng(61)
+    cov = rng.uniform(0.5, 3.0, size=M * N * T)
+    idx = np.sort(rng.choice(M * N * T, 25, replace=False))
+    out = dict(M=M, N=N, T=T, extend=ext, cov=cov, idx=idx)
+    variants = {"plain": None, "int": "int", "cov_int": (True, False), "cov_int_scale": (True, True),
+                "cov": (False, False)}
+    for name, how in variants.items():
+        g = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float), t=np.arange(T, dtype=float),
+                    extend=ext)
+        if how == "int":
+            g.addInt()
+        elif how is not None:
+            g.addCov(cov, inter=how[0], scale=how[1])
+        for tag, ii in (("sub", idx), ("all", None)):
+            S = sparse.csr_matrix(g.getS(ii))
+            S.sort_indices()
+            out[f"{name}_{tag}_data"] = S.data
+            out[f"{name}_{tag}_indices"] = S.indices.astype(np.int32)
+            out[f"{name}_{tag}_indptr"] = S.indptr.astype(np.int64)
+            out[f"{name}_{tag}_shape"] = np.array(S.shape, np.int64)
+    np.savez_compressed(os.path.join(OUT, "grid_getS.npz"), **out)
+    print("grid_getS:", {k: tuple(out[k]) for k in out if k.endswith("_all_shape")})
+
+
 def separable_cases(sp=None, only=None):
     """Separable space-time fixtures: the rho form (anisotropic, bc 1 and 3) and
     the (a, sigma) form (isotropic and half-angle; those reference classes need
@@ -318,6 +351,9 @@ def separable_cases(sp=None, only=None):
 if __name__ == "__main__":
     if len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "separable":
         separable_cases(only=sys.argv[3:] or None)
+    elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "getS":
+        getS_cases()
     else:
         main()
         separable_cases()
+        getS_cases()

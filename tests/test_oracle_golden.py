@@ -86,3 +86,24 @@ def test_facade_update_golden():
     assert abs(Q - Qg).max() <= 1e-13 * abs(Qg).max()
     mu = mod.conditional_mean(g["par"], g["y"], g["idx"], tau=float(g["tau"]))
     assert np.allclose(mu, g["mu"], rtol=1e-11, atol=1e-13)
+
+
+def test_getS_fixed_effect_columns():
+    """Grid.getS after addInt / addCov matches the reference's S bit for bit
+    (selected identity rows on a padded grid, then [1, cov], [1, cov / max],
+    [cov] or [1])."""
+    from spdepy_gb300.grids import Grid
+    g = load("grid_getS.npz")
+    M, N, T, ext = (int(g[k]) for k in ("M", "N", "T", "extend"))
+    for name in ("plain", "int", "cov_int", "cov_int_scale", "cov"):
+        grid = Grid(np.arange(M, dtype=float), np.arange(N, dtype=float), np.arange(T, dtype=float), extend=ext)
+        if name == "int":
+            grid.addInt()
+        elif name != "plain":
+            grid.addCov(g["cov"], inter=name.startswith("cov_int"), scale=name.endswith("scale"))
+        for tag, idx in (("sub", g["idx"]), ("all", None)):
+            ref = sparse.csr_matrix((g[f"{name}_{tag}_data"], g[f"{name}_{tag}_indices"], g[f"{name}_{tag}_indptr"]),
+                                    shape=tuple(g[f"{name}_{tag}_shape"]))
+            S = grid.getS(idx)
+            assert S.shape == ref.shape, (name, tag)
+            assert abs(S - ref).max() == 0.0, (name, tag)
