@@ -191,9 +191,12 @@ class Grid:
         return None
 
     def addCov(self, cov, inter=True, scale=False):
-        """Covariate (and intercept) columns of S (reference :60-64)."""
+        """Covariate (and intercept) columns of S (reference :60-64).  The
+        reference's spatial grid ignores `scale` (grids/spatial2D_regular_mesh.py:
+        55-58 never stores it), so a spatial grid keeps the unscaled covariate."""
         self.inter = inter
-        self.scale = scale
+        if self.T > 1:
+            self.scale = scale
         self.cov = np.asarray(cov, dtype=np.float64)
 
     def addInt(self):

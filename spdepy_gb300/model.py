@@ -6,11 +6,16 @@
 marginal variances diag(Q^-1) from the GPU selected inverse, replacing the
 R-INLA call of the reference (``:89-118``).  Because the factor's ordering is
 not CHOLMOD's, samples are different draws from the same distribution.
+
+With ``setModel(useCov=True)`` the latent field carries the reference's fixed
+effects (intercept and covariate coefficients, ``:129-150``); their border is
+eliminated on the host around the sparse GPU factor (``fixed_effects.py``).
 """
 from __future__ import annotations
 
 import numpy as np
 
+from .fixed_effects import Border, update_step
 from .grids import Grid
 from .optim import Optimize
 from .spdes import spde_init
@@ -37,6 +42,7 @@ class Model:
         self.tau = None
         self._obs_nodes = np.zeros(0, dtype=np.int64)
         self._obs_tau = None
+        self.border = None
 
     def model(self, spde=None, grid=None, parameters=None, ani=True, ha=True, bc=3, mod0=None):
         assert spde is not None and grid is not None
@@ -62,15 +68,40 @@ class Model:
         return res
 
     def setModel(self, mu=None, sigmas=None, useCov=None, scale=True):
-        if useCov:
-            raise NotImplementedError("covariate / intercept blocks are not on the GPU path")
-        self.mu = np.zeros(self.grid.n) if mu is None else self.grid.getS().T @ np.asarray(mu, float)
+        """Prior mean and, with useCov, the fixed effects (reference model.py:129-150):
+        two sigmas give an intercept and a covariate coefficient (the covariate is
+        `mu`, its coefficient's prior mean max(mu) when scale), one sigma an
+        intercept alone; exp(sigmas) are their prior precisions."""
+        self.useCov = useCov if useCov is not None else self.useCov
         if self.mod.Q is None:
             self.mod.setQ()
         self.Q = self.mod.Q
         self.tau = float(np.exp(self.mod.par[-1]))
         self._obs_nodes = np.zeros(0, dtype=np.int64)
         self._obs_tau = None
+        self.border = None
+        n = self.grid.n
+        if not self.useCov:
+            self.mu = np.zeros(n) if mu is None else self.grid.getS().T @ np.asarray(mu, float)
+            return
+        self.sigmas = sigmas if sigmas is not None else self.sigmas
+        if mu is None:
+            raise ValueError("the fixed-effect model needs the covariate field mu")
+        field = np.asarray(mu, float)
+        if hasattr(self.sigmas, "__len__"):
+            self.grid.addCov(field, scale=scale)
+            p = self.grid._fixed_effects().shape[1]
+            if scale:
+                self.mu = np.zeros(n + p)
+                self.mu[-2:] = [0.0, field.max()]
+            else:
+                self.mu = self.grid.getS().T @ field
+        else:
+            self.grid.addInt()
+            S = self.grid.getS()
+            self.mu = np.zeros(S.shape[1])
+            self.mu[:-1] = S[:, :-1].T @ field
+        self.border = Border(n, np.exp(np.atleast_1d(np.asarray(self.sigmas, float))))
 
     def _factor_current(self):
         plan = self.mod.plan
@@ -80,17 +111,33 @@ class Model:
             return plan.factor(True, self._obs_tau)
         return plan.factor(False, 0.0)
 
-    def sample(self, n=1, simple=False, seed=None):
-        """Draws S (mu + P L^-T z) (+ noise unless simple), reference model.py:73-87."""
+    def _solve_A(self, R):
+        """A^-1 R with the current factor (R: n x k host array)."""
         torch = _torch()
+        x, _ = self.mod.plan.solve(torch.as_tensor(np.ascontiguousarray(R, dtype=np.float64)))
+        return x.cpu().numpy()
+
+    def _sample_A(self, Z):
+        """P L^-T Z with the current factor (Z: n x k host array)."""
+        torch = _torch()
+        return self.mod.plan.sample(torch.as_tensor(np.ascontiguousarray(Z, dtype=np.float64))).cpu().numpy()
+
+    def sample(self, n=1, simple=False, seed=None):
+        """Draws S (mu + P L^-T z) (+ noise unless simple), reference model.py:73-87.
+        With fixed effects z has n + p rows and the draw covers the coefficients too."""
         if self.Q is None:
             self.setModel()
         if seed is None:
             seed = np.random.randint(100)
         nn = self.grid.n
-        z = np.random.default_rng(seed).normal(size=nn * n).reshape(nn, n)
+        p = self.border.p if self.useCov and self.border is not None else 0
+        z = np.random.default_rng(seed).normal(size=(nn + p) * n).reshape(nn + p, n)
         self._factor_current()
-        x = self.mod.plan.sample(torch.as_tensor(z)).cpu().numpy() + self.mu[:, None]
+        if p:
+            x_n, x_b = self.border.sample(self._sample_A, self._solve_A, z[:nn], z[nn:])
+            x = np.vstack([x_n, x_b]) + self.mu[:, None]
+        else:
+            x = self._sample_A(z) + self.mu[:, None]
         S = self.grid.getS()
         data = S @ x
         if not simple:
@@ -104,6 +151,8 @@ class Model:
             return z.var(axis=1)
         if self.Q is None:
             self.setModel()
+        if self.useCov:
+            raise NotImplementedError("marginal variances with fixed effects are not on the GPU path")
         self._factor_current()
         zq = self.mod.plan.selinv()
         centre = 12 if self.grid.T == 1 else 21
@@ -122,6 +171,11 @@ class Model:
         self._obs_nodes = np.concatenate([self._obs_nodes, nodes])
         self._obs_tau = tau
         self._factor_current()
+        if self.useCov and self.border is not None:
+            rows = np.arange(self.grid.M * self.grid.N * self.grid.T) if idx is None else np.asarray(idx, np.int64)
+            X = self.grid._fixed_effects()[rows]
+            self.mu = update_step(self.border, self._solve_A, self.mu, nodes, X, y, tau)
+            return
         b = np.zeros(self.grid.n)
         np.add.at(b, nodes, tau * (np.asarray(y, float) - self.mu[nodes]))
         dx, _ = self.mod.plan.solve(torch.as_tensor(b))

@@ -22,12 +22,15 @@ the CUDA path.  Cases:
   ``seperable_spatial_temporal_idiffusion2D.py``).  They pin the oracle only; the
   CUDA path does not cover this family yet, so they carry their own prefix.
 
+* ``facade_cov``  ``Model.setModel(useCov=True)`` and two ``update`` calls, with
+  covariate + intercept and with intercept only (reference ``model.py:120-150``).
 * ``grid_getS``  the observation matrix with fixed-effect columns: ``Grid.getS``
   after ``addInt`` / ``addCov`` (with and without intercept and scaling) on a
   padded space-time grid (reference ``grids/spat2Dtemp_regular_mesh.py:35-68``).
 
 ``python tests/golden/make_golden.py --only separable [name ...]`` regenerates just
-the separable cases, ``--only getS`` the grid_getS fixture.
+the separable cases, ``--only getS`` the grid_getS fixture, ``--only facade_cov`` the
+facade_cov fixture.
 """
 from __future__ import annotations
 
@@ -273,6 +276,36 @@ def main():
     print("facade_wm: mu norm", np.linalg.norm(model.mu))
 
 
+def facade_cov_case(sp=None):
+    """Model.setModel(useCov=True) and two updates on a stationary Whittle-Matern
+    field: the covariate form (two sigmas: intercept + scaled covariate, prior
+    mean of the covariate coefficient max(cov)) and the intercept-only form (one
+    sigma) (reference model.py:120-150)."""
+    sp = sp or ref_harness.load_reference()
+    M, N = 16, 14
+    par = np.array([-0.6, 0.1, 0.2, 0.4, 2.0])
+    rng = np.random.default_rng(71)
+    cov = 1.0 + rng.uniform(0.0, 2.0, size=M * N)
+    idx1 = np.sort(rng.choice(M * N, 30, replace=False))
+    idx2 = np.sort(rng.choice(M * N, 25, replace=False))
+    y1 = rng.normal(size=30) + 2.0
+    y2 = rng.normal(size=25) + 2.0
+    out = dict(M=M, N=N, par=par, cov=cov, idx1=idx1, idx2=idx2, y1=y1, y2=y2)
+    for name, sig in (("cov", np.log(np.array([0.01, 140.0]))), ("int", np.log(0.5))):
+        g = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float))
+        model = sp.Model(spde="whittle-matern", grid=g, parameters=par, ani=True, ha=False, bc=3)
+        model.setModel(mu=cov, sigmas=sig, useCov=True, scale=True)
+        out[f"{name}_sigmas"] = np.atleast_1d(sig)
+        out[f"{name}_mu0"] = model.mu.copy()
+        out[f"{name}_tau"] = float(model.tau)
+        model.update(y1, idx1)
+        out[f"{name}_mu1"] = model.mu.copy()
+        model.update(y2, idx2)
+        out[f"{name}_mu2"] = model.mu.copy()
+    np.savez_compressed(os.path.join(OUT, "facade_cov.npz"), **out)
+    print("facade_cov:", {k: out[k].shape for k in out if k.endswith("_mu2")})
+
+
 def getS_cases(sp=None):
     """Grid.getS with fixed-effect columns on a padded space-time grid."""
     sp = sp or ref_harness.load_reference()
@@ -353,7 +386,10 @@ if __name__ == "__main__":
         separable_cases(only=sys.argv[3:] or None)
     elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "getS":
         getS_cases()
+    elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "facade_cov":
+        facade_cov_case()
     else:
         main()
         separable_cases()
         getS_cases()
+        facade_cov_case()

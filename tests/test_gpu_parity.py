@@ -180,6 +180,27 @@ def test_facade_update_golden():
     assert np.allclose(m.mu, g["mu"], rtol=1e-10, atol=1e-12)
 
 
+@pytest.mark.parametrize("name", ["cov", "int"])
+def test_facade_fixed_effects_golden(name):
+    """Model.setModel(useCov=True) and two updates on the GPU factor, with the
+    fixed-effect border eliminated on the host, against the reference's
+    augmented Cholesky solves (covariate + intercept, and intercept alone)."""
+    import spdepy_gb300 as sp
+    g = load("facade_cov.npz")
+    M, N = int(g["M"]), int(g["N"])
+    grid = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float))
+    m = sp.Model(spde="whittle-matern", grid=grid, parameters=g["par"], ani=True, ha=False, bc=3, precision="fp64")
+    sig = g["cov_sigmas"] if name == "cov" else float(g["int_sigmas"][0])
+    m.setModel(mu=g["cov"], sigmas=sig, useCov=True, scale=True)
+    assert np.allclose(m.mu, g[f"{name}_mu0"], rtol=1e-14, atol=0)
+    for k in (1, 2):
+        m.update(g[f"y{k}"], g[f"idx{k}"])
+        ref = g[f"{name}_mu{k}"]
+        assert np.allclose(m.mu, ref, rtol=1e-9, atol=1e-11 * np.abs(ref).max()), k
+    draws = m.sample(n=8, simple=True, seed=3)
+    assert draws.shape == (M * N, 8) and np.isfinite(draws).all()
+
+
 def test_factor_handle_survives_other_factorisations():
     """makeQ's factor handle (the reference's cholesky(Q)) keeps solving with Q
     after the plan has factored Q + tau S^T S and run a log-likelihood, and

@@ -107,3 +107,72 @@ def test_getS_fixed_effect_columns():
             S = grid.getS(idx)
             assert S.shape == ref.shape, (name, tag)
             assert abs(S - ref).max() == 0.0, (name, tag)
+
+
+def _fixed_effect_setup(g, name):
+    """Grid with the fixture's fixed-effect columns and the reference's initial mu (model.py:129-150)."""
+    from spdepy_gb300.grids import Grid
+    M, N = int(g["M"]), int(g["N"])
+    grid = Grid(np.arange(M, dtype=float), np.arange(N, dtype=float))
+    cov = g["cov"]
+    n = grid.n
+    if name == "cov":
+        grid.addCov(cov, scale=True)
+        mu = np.zeros(n + 2)
+        mu[-2:] = [0.0, cov.max()]
+    else:
+        grid.addInt()
+        S = grid.getS()
+        mu = np.zeros(n + 1)
+        mu[:-1] = S[:, :-1].T @ cov
+    return grid, mu
+
+
+@pytest.mark.parametrize("name", ["cov", "int"])
+def test_fixed_effect_updates_by_block_elimination(name):
+    """Model.update with fixed effects (intercept and covariate coefficients) by
+    block elimination on the sparse part matches the reference's augmented
+    Cholesky solves (dense exact solves stand in for the GPU factor here)."""
+    from oracle.spde_oracle import OracleGrid, OracleModel
+    from spdepy_gb300.fixed_effects import Border, update_step
+    g = load("facade_cov.npz")
+    M, N = int(g["M"]), int(g["N"])
+    Q = OracleModel(OracleGrid(np.arange(M, dtype=float), np.arange(N, dtype=float)), "whittle-matern", "ani",
+                    3).makeQ(g["par"]).toarray()
+    grid, mu = _fixed_effect_setup(g, name)
+    assert np.allclose(mu, g[f"{name}_mu0"], rtol=1e-14, atol=0)
+    tau = float(g[f"{name}_tau"])
+    border = Border(grid.n, np.exp(g[f"{name}_sigmas"]))
+    A = Q.copy()
+    F = grid._fixed_effects()
+    for k in (1, 2):
+        idx, y = g[f"idx{k}"], g[f"y{k}"]
+        nodes = grid.obs_nodes(idx)
+        np.add.at(A, (nodes, nodes), tau)
+        mu = update_step(border, lambda R: np.linalg.solve(A, R), mu, nodes, F[idx], y, tau)
+        ref = g[f"{name}_mu{k}"]
+        assert np.allclose(mu, ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max()), k
+
+
+def test_fixed_effect_draws_have_the_augmented_covariance():
+    """Border.sample: x = (P L^-T z_n - A^-1 B x_b, L_Sc^-T z_b) has covariance
+    exactly Q_aug^-1, checked with the draw's linear map on a small dense case."""
+    from spdepy_gb300.fixed_effects import Border
+    rng = np.random.default_rng(5)
+    n, p = 30, 2
+    R = rng.normal(size=(n, n))
+    A0 = R @ R.T + n * np.eye(n)
+    border = Border(n, [0.5, 2.0])
+    nodes = rng.choice(n, 12, replace=False)
+    X = rng.normal(size=(12, p))
+    border.add(nodes, X, 3.0)
+    A = A0.copy()
+    np.add.at(A, (nodes, nodes), 3.0)
+    L = np.linalg.cholesky(A)
+    import scipy.linalg as sla
+    Zn, Zb = np.eye(n + p)[:n], np.eye(n + p)[n:]  # the map applied to the identity
+    xn, xb = border.sample(lambda Z: sla.solve_triangular(L.T, Z, lower=False), lambda R: np.linalg.solve(A, R),
+                           Zn, Zb)
+    G = np.vstack([xn, xb])  # x = G z
+    Qaug = np.block([[A, border.B], [border.B.T, border.C]])
+    assert np.allclose(G @ G.T, np.linalg.inv(Qaug), rtol=1e-9, atol=1e-12)
