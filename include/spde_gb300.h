@@ -61,7 +61,11 @@ typedef struct {
  * with nk = nbasis if var_h else 1 and nw = 2 (constant velocity), 2*nbasis
  * (B-spline velocity), 1 (lambda times a given field) or 0 (spatial model).
  * The last five entries before log tau describe the initial-field
- * Whittle-Matern model of spatio-temporal models and are ignored when T == 1. */
+ * Whittle-Matern model of spatio-temporal models and are ignored when T == 1.
+ * Separable models Q = Qt (x) Qs (spdes/seperable_spatial_temporal{,_ha,
+ * _idiffusion}2D.py) use the spatial layout (adv = 0, Qs = A^T V^-1 A with
+ * A = V kappa - A_H) and put their temporal parameters in the log sigma slot
+ * (log rho, or a) and the log kappa0 slot (log sigma of the (a, sigma) form). */
 typedef struct {
   int32_t Mx, Ny, T;
   int32_t bc;           /* 1: Neumann (zero flux), 3: Dirichlet (zero) */
@@ -76,6 +80,7 @@ typedef struct {
   const double* ww;     /* host, Ns x 4 given face velocities          (adv == 3) */
   int32_t mod0_diff_form;
   int32_t mod0_bc;
+  int32_t temporal;     /* separable plans only: 1 AR(1) in log rho, 2 (a, log sigma); 0 otherwise */
 } SpdeModelDesc;
 
 /* ---- B3: stencil triplets.  Replace the ctypes calls
@@ -98,6 +103,12 @@ int spde_advection_triplets(int M, int N, const double* G, const double* dG, int
  * arenas (assembly, products and PCG only); factor-based calls then return
  * SPDE_ERR_STATE. */
 int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out);
+/* Plan for separable space-time models Q = Qt (x) Qs (the reference's
+ * SeperableSpatialTemporal{,Ha,IDiffusion}2D, spdes/seperable_spatial_temporal2D.py:
+ * 64-83): every time slice couples to its neighbours through the 25-point Qs, a
+ * 75-slot stencil.  T >= 2; precision FP64 or mixed.  The learned preconditioner
+ * and spde_qsqrt return SPDE_ERR_STATE on such plans. */
+int spde_plan_create_separable(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out);
 int spde_plan_destroy(SpdePlan* plan);
 int spde_plan_set_stream(SpdePlan* plan, void* stream);
 int spde_plan_info(const SpdePlan* plan, SpdePlanInfo* info);

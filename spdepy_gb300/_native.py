@@ -40,7 +40,7 @@ class ModelDesc(ctypes.Structure):
                 ("diff_form", ctypes.c_int32), ("var_h", ctypes.c_int32), ("adv", ctypes.c_int32),
                 ("nbasis", ctypes.c_int32), ("bs", ctypes.c_void_p), ("bsH", ctypes.c_void_p),
                 ("bsA", ctypes.c_void_p), ("ww", ctypes.c_void_p), ("mod0_diff_form", ctypes.c_int32),
-                ("mod0_bc", ctypes.c_int32)]
+                ("mod0_bc", ctypes.c_int32), ("temporal", ctypes.c_int32)]
 
 
 _lib = None
@@ -51,6 +51,7 @@ SIGNATURES = {
     "spde_diffusion_triplets": (_I, [_I, _I, _P, _I, _D, _D, _I, _P, _P, _P, _P]),
     "spde_advection_triplets": (_I, [_I, _I, _P, _P, _I, _D, _D, _I, _I, _P, _P, _P, _P]),
     "spde_plan_create": (_I, [_I, _I, _I, _I, _I, ctypes.POINTER(_P)]),
+    "spde_plan_create_separable": (_I, [_I, _I, _I, _I, _I, ctypes.POINTER(_P)]),
     "spde_plan_destroy": (_I, [_P]),
     "spde_plan_set_stream": (_I, [_P, _P]),
     "spde_plan_info": (_I, [_P, ctypes.POINTER(PlanInfo)]),

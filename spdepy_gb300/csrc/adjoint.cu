@@ -369,10 +369,79 @@ int noalloc_scratch(double** ptr, int64_t* elems) {
   return 0;
 }
 
+// --- separable models Q = Qt (x) Qs.  Per cell c: the spatial cotangent
+// Gs(c, s) = sum_t sum_dt Qt(t, t + dt) Gbar(t, c, dt, s) into red[c 84 + s]
+// (the spatial adjoint then gives every Qs parameter), and the partial sums
+// sum_s Gbar-class(c, s) Qs(c, s) for the end-diagonal, interior-diagonal and
+// off-diagonal classes of Qt into red[c 84 + 25 .. 27].
+__global__ void sep_reduce_kernel(int Ns, int T, double qe, double qm, double qo, const double* __restrict__ gbar,
+                                  const double* __restrict__ Qs, double* __restrict__ red) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= Ns) return;
+  double* r = red + int64_t(c) * 84;
+  double pe = 0.0, pm = 0.0, po = 0.0;
+  for (int s = 0; s < 25; ++s) {
+    double ee = 0.0, em = 0.0, eo = 0.0;
+    for (int t = 0; t < T; ++t) {
+      const double* g = gbar + (int64_t(t) * Ns + c) * 75;
+      if (t == 0 || t == T - 1) ee += g[25 + s];
+      else em += g[25 + s];
+      eo += g[s] + g[50 + s];  // slots outside the lattice hold zero
+    }
+    r[s] = qe * ee + qm * em + qo * eo;
+    const double q = Qs[int64_t(c) * 25 + s];
+    pe += ee * q;
+    pm += em * q;
+    po += eo * q;
+  }
+  r[25] = pe;
+  r[26] = pm;
+  r[27] = po;
+}
+
+// Gradient of the two temporal parameters: sum_c of the partials, weighted by
+// the derivatives of (end, interior, off) of Qt; one block.
+__global__ void sep_temporal_kernel(int Ns, const double* __restrict__ red, double a0, double a1, double a2,
+                                    double b0, double b1, double b2, double* __restrict__ grad) {
+  __shared__ double sh[3][256];
+  double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+  for (int c = threadIdx.x; c < Ns; c += 256) {
+    const double* r = red + int64_t(c) * 84;
+    e0 += r[25];
+    e1 += r[26];
+    e2 += r[27];
+  }
+  sh[0][threadIdx.x] = e0;
+  sh[1][threadIdx.x] = e1;
+  sh[2][threadIdx.x] = e2;
+  __syncthreads();
+  for (int q = 128; q > 0; q >>= 1) {
+    if (threadIdx.x < q)
+      for (int i = 0; i < 3; ++i) sh[i][threadIdx.x] += sh[i][threadIdx.x + q];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    grad[0] = a0 * sh[0][0] + a1 * sh[1][0] + a2 * sh[2][0];
+    grad[1] = b0 * sh[0][0] + b1 * sh[1][0] + b2 * sh[2][0];
+  }
+}
+
 void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st) {
   const int Ns = p->sym.Mx * p->sym.Ny;
   double* red = work;
   double* cg = work + int64_t(Ns) * 84;
+  if (p->temporal) {
+    const DevModel ms = spatial_view(p->model);
+    const int to = 4 * ms.nk + ms.nw;
+    double qt[3], d1[3], d2[3];
+    separable_qt(p->temporal, p->theta[to], p->theta[to + 1], qt, d1, d2);
+    sep_reduce_kernel<<<(Ns + 127) / 128, 128, 0, st>>>(Ns, p->sym.T, qt[0], qt[1], qt[2], gbar, p->d_QA, red);
+    cell_adjoint_kernel<<<(Ns + 127) / 128, 128, 0, st>>>(ms, red, p->d_Ageo, p->d_A0geo, p->d_kap, p->d_qs, 1.0,
+                                                           cg);
+    coef_reduce_kernel<<<4 * ms.nk + ms.nw + 5, 256, 0, st>>>(ms, cg, grad_dev);
+    sep_temporal_kernel<<<1, 256, 0, st>>>(Ns, red, d1[0], d1[1], d1[2], d2[0], d2[1], d2[2], grad_dev + to);
+    return;
+  }
   int64_t tot = int64_t(Ns) * 34;
   time_reduce_kernel<<<int((tot + 255) / 256), 256, 0, st>>>(Ns, p->sym.T, p->sym.nslots, gbar, red);
   cell_adjoint_kernel<<<(Ns + 127) / 128, 128, 0, st>>>(p->model, red, p->d_Ageo, p->d_A0geo, p->d_kap, p->d_qs,

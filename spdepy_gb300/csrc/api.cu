@@ -68,13 +68,6 @@ __global__ void obs_resid_kernel(const int* __restrict__ idx, int m, int r, cons
   d[e] = y[e] - mu[int64_t(idx[e / r]) * r + e % r];
 }
 
-__device__ __forceinline__ void slot_geo(int T, int s, int* dx, int* dy, int* dt) {
-  if (T == 1) { *dt = 0; *dy = s / 5 - 2; *dx = s % 5 - 2; return; }
-  if (s < 9) { *dt = -1; *dy = s / 3 - 1; *dx = s % 3 - 1; }
-  else if (s < 34) { *dt = 0; *dy = (s - 9) / 5 - 2; *dx = (s - 9) % 5 - 2; }
-  else { *dt = 1; *dy = (s - 34) / 3 - 1; *dx = (s - 34) % 3 - 1; }
-}
-
 // Gbar = a * (ZQ - ZQc) - 1/2 sum_c mu mu^T on the stencil (exact traces), or with
 // Hutchinson probes: a/nh1 * sym(Delta V^T) where Delta = TrQ - TrQc.
 __global__ void gbar_kernel(int Mx, int Ny, int T, int nslots, double a, const double* __restrict__ zq,
@@ -86,7 +79,7 @@ __global__ void gbar_kernel(int Mx, int Ny, int T, int nslots, double a, const d
   if (e >= n * nslots) return;
   const int k = int(e / nslots), s = int(e % nslots);
   int dx, dy, dt;
-  slot_geo(T, s, &dx, &dy, &dt);
+  stencil_slot(nslots, s, &dx, &dy, &dt);
   const int t = k / (Mx * Ny), c = k - t * Mx * Ny, y = c / Mx, x = c - y * Mx;
   if (x + dx < 0 || x + dx >= Mx || y + dy < 0 || y + dy >= Ny || t + dt < 0 || t + dt >= T) {
     g[e] = 0.0;
@@ -326,6 +319,8 @@ static void share_model(const Plan& p, Plan& t) {
   t.model_set = p.model_set;
   t.d_Q0 = p.d_Q0; t.d_QA = p.d_QA; t.d_QO = p.d_QO; t.d_cQs = p.d_cQs;
   t.cfac = p.cfac;
+  t.temporal = p.temporal;
+  t.qt[0] = p.qt[0]; t.qt[1] = p.qt[1]; t.qt[2] = p.qt[2];
   t.assembled = p.assembled;
   t.d_obs_cnt = p.d_obs_cnt;
   t.d_obs_idx = p.d_obs_idx;
@@ -334,13 +329,22 @@ static void share_model(const Plan& p, Plan& t) {
   t.profile_tc_only = p.profile_tc_only;
 }
 
+// The learned preconditioner reads the 43-slot spatio-temporal stencil and the
+// square root of Q is the implicit-Euler factor: neither applies to separable plans.
+static int not_separable(Plan& p, const char* what) {
+  if (p.sym.nslots != kSlotsSep) return SPDE_OK;
+  p.last_error = std::string(what) + " is not available for separable models";
+  return SPDE_ERR_STATE;
+}
+
 static int no_factor(SpdePlan* plan) {
   plan->p.last_error = "this plan was created for iterative solves only (no factorisation)";
   return SPDE_ERR_STATE;
 }
 
-int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out) {
+static int plan_create(int Mx, int Ny, int T, int precision, int leaf_max, bool separable, SpdePlan** out) {
   if (!out || precision < 0 || precision > 2) return SPDE_ERR_ARG;
+  if (separable && (precision == SPDE_PRECISION_ITERATIVE || T < 2)) return SPDE_ERR_ARG;
   *out = nullptr;
   SpdePlan* plan = new (std::nothrow) SpdePlan();
   if (!plan) return SPDE_ERR_NO_MEMORY;
@@ -356,7 +360,7 @@ int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePla
     *out = plan;
     return SPDE_OK;
   }
-  if (build_symbolic(Mx, Ny, T, leaf_max > 0 ? leaf_max : 128, 64, &plan->p.sym) != 0) {
+  if (build_symbolic(Mx, Ny, T, leaf_max > 0 ? leaf_max : 128, 64, &plan->p.sym, separable) != 0) {
     delete plan;
     return SPDE_ERR_ARG;
   }
@@ -367,6 +371,14 @@ int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePla
   }
   *out = plan;
   return SPDE_OK;
+}
+
+int spde_plan_create(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out) {
+  return plan_create(Mx, Ny, T, precision, leaf_max, false, out);
+}
+
+int spde_plan_create_separable(int Mx, int Ny, int T, int precision, int leaf_max, SpdePlan** out) {
+  return plan_create(Mx, Ny, T, precision, leaf_max, true, out);
 }
 
 int spde_plan_destroy(SpdePlan* plan) {
@@ -472,7 +484,20 @@ int spde_set_model(SpdePlan* plan, const SpdeModelDesc* d) {
     p.last_error = "unsupported model flags";
     return SPDE_ERR_ARG;
   }
-  if ((d->T == 1) != (d->adv == 0)) { p.last_error = "spatial models have no advection, spatio-temporal ones do"; return SPDE_ERR_ARG; }
+  const bool sep = p.sym.nslots == kSlotsSep;
+  if (sep) {
+    if (d->adv != 0 || (d->temporal != 1 && d->temporal != 2)) {
+      p.last_error = "a separable plan needs a model without advection and temporal = 1 (rho) or 2 (a, sigma)";
+      return SPDE_ERR_ARG;
+    }
+  } else if (d->temporal != 0) {
+    p.last_error = "separable models need a plan from spde_plan_create_separable";
+    return SPDE_ERR_ARG;
+  } else if ((d->T == 1) != (d->adv == 0)) {
+    p.last_error = "spatial models have no advection, spatio-temporal ones do";
+    return SPDE_ERR_ARG;
+  }
+  p.temporal = d->temporal;
   const int Ns = d->Mx * d->Ny;
   const int nb = std::max(d->nbasis, 1);
   auto up = [&](double*& dst, const double* src, size_t n) -> int {
@@ -522,10 +547,25 @@ int spde_assemble(SpdePlan* plan, const double* theta, int ntheta) {
     if (!std::isfinite(theta[i])) { p.last_error = "non-finite parameter"; return SPDE_ERR_ARG; }
   p.theta.assign(theta, theta + ntheta);
   API_CUDA(cudaMemcpyAsync(p.d_theta, theta, ntheta * sizeof(double), cudaMemcpyHostToDevice, p.stream));
-  const double lsig = theta[4 * p.model.nk + p.model.nw];
-  p.cfac = p.sym.T > 1 ? 1.0 / (p.model.dt * std::exp(lsig)) : 1.0;
-  launch_fields(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.stream);
-  launch_qstencil(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.cfac, p.stream);
+  const int to = 4 * p.model.nk + p.model.nw;  // log sigma, or the first temporal parameter
+  if (p.temporal) {
+    // Q = Qt (x) Qs: Qs through the spatial assembly, Qt from the temporal
+    // parameters (spdes/seperable_spatial_temporal2D.py:186-212,
+    // seperable_spatial_temporal_idiffusion2D.py:166-189)
+    if (!separable_qt(p.temporal, theta[to], theta[to + 1], p.qt)) {
+      p.last_error = "rho = exp(par) must be below 1";
+      return SPDE_ERR_ARG;
+    }
+    p.cfac = 1.0;
+    const DevModel ms = spatial_view(p.model);
+    launch_fields(ms, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.stream);
+    launch_qstencil(ms, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, 1.0, p.stream);
+  } else {
+    p.cfac = p.sym.T > 1 ? 1.0 / (p.model.dt * std::exp(theta[to])) : 1.0;
+    launch_fields(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.stream);
+    launch_qstencil(p.model, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.cfac,
+                    p.stream);
+  }
   p.launches_total += 2;
   API_CUDA(cudaGetLastError());
   p.assembled = true;
@@ -761,7 +801,7 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   launch_adjoint(&p, S.gbar.p, S.gradv.p, S.work.p, st);
   std::vector<double> g(ntheta, 0.0);
   API_CUDA(cudaMemcpyAsync(g.data(), S.gradv.p, (ntheta - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
-  const int centre = p.sym.T == 1 ? 12 : 21;
+  const int centre = p.sym.nslots / 2;  // the (0, 0, 0) slot of every layout
   obs_trace_kernel<<<nblk, 256, 0, st>>>(p.d_obs_idx, m, exact ? S.zqc.p : nullptr, ns, centre, S.trc.p, V, nh1,
                                          S.part.p);
   const double tr = host_sum_partials(S.part.p, nblk, st);
@@ -787,6 +827,7 @@ int spde_precond_nparams(void) { return kPcParams; }
 int spde_precond_weights(SpdePlan* plan, int with_obs, double tau, const float* params, float* w, float* act) {
   if (!plan || !params || !w) return SPDE_ERR_ARG;
   Plan& p = plan->p;
+  if (int rc = not_separable(p, "the learned preconditioner")) return rc;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   return pc_weights(&p, with_obs, tau, params, w, act) ? SPDE_ERR_CUDA : SPDE_OK;
@@ -796,6 +837,7 @@ int spde_precond_grad(SpdePlan* plan, int with_obs, double tau, const float* par
                       const float* act, const double* z, int k, double* loss, float* grad) {
   if (!plan || !params || !w || !act || !z || k < 1 || !loss || !grad) return SPDE_ERR_ARG;
   Plan& p = plan->p;
+  if (int rc = not_separable(p, "the learned preconditioner")) return rc;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   const int rc = pc_grad(&p, with_obs, tau, params, w, act, z, k, loss, grad);
@@ -815,6 +857,7 @@ int spde_adam_step(SpdePlan* plan, float* params, const float* grad, float* m, f
 int spde_qsqrt(SpdePlan* plan, int transpose, const double* x, double* y, int nrhs) {
   if (!plan || !x || !y || nrhs < 1) return SPDE_ERR_ARG;
   Plan& p = plan->p;
+  if (int rc = not_separable(p, "the square root of Q")) return rc;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   const int rc = qsqrt_apply(&p, transpose, x, y, nrhs);
   if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
@@ -838,6 +881,8 @@ int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, co
       (precond == 2 && (!w_q || !w_qc)))
     return SPDE_ERR_ARG;
   Plan& p = plan->p;
+  if (precond == 2)
+    if (int rc = not_separable(p, "the learned preconditioner")) return rc;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   if (!p.d_obs_idx || p.nobs < 1) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   cudaStream_t st = p.stream;
@@ -886,7 +931,7 @@ int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, co
   launch_adjoint(&p, S.gbar.p, S.gradv.p, S.work.p, st);
   std::vector<double> g(ntheta, 0.0);
   API_CUDA(cudaMemcpyAsync(g.data(), S.gradv.p, (ntheta - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
-  const int centre = p.sym.T == 1 ? 12 : 21;
+  const int centre = p.sym.nslots / 2;  // the (0, 0, 0) slot of every layout
   obs_trace_kernel<<<nblk, 256, 0, st>>>(p.d_obs_idx, m, nullptr, ns, centre, S.trc.p, V, nh1, S.part.p);
   const double tr = host_sum_partials(S.part.p, nblk, st);
   API_CUDA(cudaGetLastError());
@@ -902,6 +947,8 @@ int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float*
       (precond == 2 && !w))
     return SPDE_ERR_ARG;
   Plan& p = plan->p;
+  if (precond == 2)
+    if (int rc = not_separable(p, "the learned preconditioner")) return rc;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   const int rc = pcg_solve(&p, with_obs, tau, precond, w, b, x, nrhs, tol, maxit, 8, iters, relres);

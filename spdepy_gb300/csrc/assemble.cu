@@ -163,13 +163,6 @@ __global__ void qstencil_kernel(DevModel m, const double* __restrict__ Ageo, con
   cQs[c] = cfac * qs[c];
 }
 
-__device__ __forceinline__ void slot_off(int T, int s, int* dx, int* dy, int* dt) {
-  if (T == 1) { *dt = 0; *dy = s / 5 - 2; *dx = s % 5 - 2; return; }
-  if (s < 9) { *dt = -1; *dy = s / 3 - 1; *dx = s % 3 - 1; }
-  else if (s < 34) { *dt = 0; *dy = (s - 9) / 5 - 2; *dx = (s - 9) % 5 - 2; }
-  else { *dt = 1; *dy = (s - 34) / 3 - 1; *dx = (s - 34) % 3 - 1; }
-}
-
 // Q in stencil layout (natural order, nslots values per node), FP64.
 __global__ void qexport_kernel(QStencil q, int nslots, const int* __restrict__ obs_cnt, double tau,
                                double* __restrict__ out) {
@@ -180,7 +173,7 @@ __global__ void qexport_kernel(QStencil q, int nslots, const int* __restrict__ o
   const int t = k / q.Ns, c = k - t * q.Ns;
   const int y = c / q.Mx, x = c - y * q.Mx;
   int dx, dy, dt;
-  slot_off(q.T, s, &dx, &dy, &dt);
+  stencil_slot(nslots, s, &dx, &dy, &dt);
   double v = 0.0;
   if (x + dx >= 0 && x + dx < q.Mx && y + dy >= 0 && y + dy < q.Ny && t + dt >= 0 && t + dt < q.T) {
     v = qval(q, c, t, dx, dy, dt);
@@ -202,7 +195,7 @@ __global__ void scatter_kernel(QStencil q, int nslots, const int* __restrict__ a
   const int k = int(e / nslots), s = int(e % nslots);
   const int t = k / q.Ns, c = k - t * q.Ns;
   int dx, dy, dt;
-  slot_off(q.T, s, &dx, &dy, &dt);
+  stencil_slot(nslots, s, &dx, &dy, &dt);
   double v = qval(q, c, t, dx, dy, dt);
   if (obs_cnt && dx == 0 && dy == 0 && dt == 0) v += tau * obs_cnt[k];
   const DevFront f = fronts[front_of[perm[k]]];
@@ -361,10 +354,50 @@ __global__ void __launch_bounds__(128) spmv_cells_kernel(QStencil q, const int* 
   }
 }
 
+// Separable Q = Qt (x) Qs: one thread per spatial cell and right-hand side forms
+// the spatial product u_t = sum_s Qs[c, s] x_t(c + off_s) once per time slice and
+// combines y_t = Qt_tt u_t + Qt_off (u_(t-1) + u_(t+1)).
+__global__ void __launch_bounds__(128) spmv_sep_kernel(QStencil q, const int* __restrict__ obs, double tau,
+                                                       const double* __restrict__ x, double* __restrict__ y,
+                                                       int nrhs) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= int64_t(q.Ns) * nrhs) return;
+  const int c = int(e / nrhs), r = int(e - int64_t(c) * nrhs);
+  const int cy = c / q.Mx, cx = c - cy * q.Mx;
+  double qa[25];
+  uint32_t m25 = 0;
+#pragma unroll
+  for (int s = 0; s < 25; ++s) {
+    const int dx = s % 5 - 2, dy = s / 5 - 2;
+    const bool in = cx + dx >= 0 && cx + dx < q.Mx && cy + dy >= 0 && cy + dy < q.Ny;
+    m25 |= uint32_t(in) << s;
+    qa[s] = q.QA[int64_t(c) * 25 + s];
+  }
+  auto spatial = [&](int t) {
+    const double* xt = x + (int64_t(t) * q.Ns + c) * nrhs + r;
+    double acc = 0.0;
+#pragma unroll
+    for (int s = 0; s < 25; ++s)
+      if (m25 >> s & 1u) acc = fma(qa[s], xt[int64_t((s / 5 - 2) * q.Mx + (s % 5 - 2)) * nrhs], acc);
+    return acc;
+  };
+  double up = 0.0, uc = spatial(0);
+  for (int t = 0; t < q.T; ++t) {
+    const double un = t + 1 < q.T ? spatial(t + 1) : 0.0;
+    const int64_t k = int64_t(t) * q.Ns + c;
+    double acc = (t == 0 || t == q.T - 1 ? q.qt_end : q.qt_mid) * uc + q.qt_off * (up + un);
+    if (obs) acc = fma(tau * obs[k], x[k * nrhs + r], acc);
+    y[k * nrhs + r] = acc;
+    up = uc;
+    uc = un;
+  }
+}
+
 void launch_spmv(const QStencil& q, const int* obs, double tau, const double* x, double* y, int nrhs,
                  cudaStream_t st) {
   const int64_t tot = int64_t(q.Ns) * nrhs;
-  spmv_cells_kernel<<<nblk(tot, 128), 128, 0, st>>>(q, obs, tau, x, y, nrhs);
+  if (q.sep) spmv_sep_kernel<<<nblk(tot, 128), 128, 0, st>>>(q, obs, tau, x, y, nrhs);
+  else spmv_cells_kernel<<<nblk(tot, 128), 128, 0, st>>>(q, obs, tau, x, y, nrhs);
 }
 void launch_diffusion_triplets(int M, int N, const double* H, int field, double hx, double hy, int bc, int* row,
                                int* col, double* val, cudaStream_t st) {

@@ -30,15 +30,33 @@ struct DevModel {
 // Compact Q: per-cell spatial stencils (see assemble.cu).
 struct QStencil {
   const double* Q0;   // Ns x 25: first diagonal block minus c*Qs (mod0's A0^T V^-1 A0)
-  const double* QA;   // Ns x 25: c * A^T (Qs/V^2) A   (T == 1: A^T V^-1 A)
+  const double* QA;   // Ns x 25: c * A^T (Qs/V^2) A   (T == 1 or separable: A^T V^-1 A)
   const double* QO;   // Ns x 9 : -c Qs V^-1 A, block (t, t+1)
   const double* cQs;  // Ns     : c * V kappa^2
   int Mx, Ny, T, Ns;
+  // separable space-time models, Q = Qt (x) Qs with Qs = QA and the tridiagonal
+  // Qt given by its end and interior diagonal and its off-diagonal
+  int sep = 0;
+  double qt_end = 0.0, qt_mid = 0.0, qt_off = 0.0;
 };
 
 #ifdef __CUDACC__
+// Offset (dx, dy, dt) of slot s in the layout with `nslots` slots (25: spatial,
+// 43: spatio-temporal, 75: separable; see spde_internal.h).
+__device__ __forceinline__ void stencil_slot(int nslots, int s, int* dx, int* dy, int* dt) {
+  if (nslots == 25) { *dt = 0; *dy = s / 5 - 2; *dx = s % 5 - 2; return; }
+  if (nslots == 75) { *dt = s / 25 - 1; const int r = s % 25; *dy = r / 5 - 2; *dx = r % 5 - 2; return; }
+  if (s < 9) { *dt = -1; *dy = s / 3 - 1; *dx = s % 3 - 1; }
+  else if (s < 34) { *dt = 0; *dy = (s - 9) / 5 - 2; *dx = (s - 9) % 5 - 2; }
+  else { *dt = 1; *dy = (s - 34) / 3 - 1; *dx = (s - 34) % 3 - 1; }
+}
+
 // Value of Q at node (cell c, time t), stencil offset (dx, dy, dt).
 __device__ __forceinline__ double qval(const QStencil& q, int c, int t, int dx, int dy, int dt) {
+  if (q.sep) {
+    const double w = dt != 0 ? q.qt_off : (t == 0 || t == q.T - 1 ? q.qt_end : q.qt_mid);
+    return w * q.QA[int64_t(c) * 25 + (dy + 2) * 5 + dx + 2];
+  }
   if (q.T == 1) return q.QA[int64_t(c) * 25 + (dy + 2) * 5 + dx + 2];
   if (dt == 0) {
     const int s = (dy + 2) * 5 + dx + 2;

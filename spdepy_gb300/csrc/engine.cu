@@ -714,17 +714,14 @@ __global__ void zsym_kernel(int Mx, int Ny, int T, int nslots, const int* __rest
   if (amap[e] >= 0) return;
   const int k = int(e / nslots), s = int(e % nslots);
   int dx, dy, dt;
-  if (T == 1) { dt = 0; dy = s / 5 - 2; dx = s % 5 - 2; }
-  else if (s < 9) { dt = -1; dy = s / 3 - 1; dx = s % 3 - 1; }
-  else if (s < 34) { dt = 0; dy = (s - 9) / 5 - 2; dx = (s - 9) % 5 - 2; }
-  else { dt = 1; dy = (s - 34) / 3 - 1; dx = (s - 34) % 3 - 1; }
+  stencil_slot(nslots, s, &dx, &dy, &dt);
   const int t = k / (Mx * Ny), c = k - t * Mx * Ny, y = c / Mx, x = c - y * Mx;
   if (x + dx < 0 || x + dx >= Mx || y + dy < 0 || y + dy >= Ny || t + dt < 0 || t + dt >= T) {
     zq[e] = 0.0;
     return;
   }
   const int64_t nb = (int64_t(t + dt) * Ny + y + dy) * Mx + x + dx;
-  const int opp = (T == 1 ? 24 : 42) - s;
+  const int opp = nslots - 1 - s;  // every layout is symmetric under (dx, dy, dt) -> -(dx, dy, dt)
   zq[e] = zq[nb * nslots + opp];
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <map>
 #include <memory>
 #include <string>
@@ -75,6 +76,46 @@ struct Schedule {
   void release();
 };
 
+// Separable models Q = Qt (x) Qs: the tridiagonal AR(1) precision Qt as its end
+// diagonal, interior diagonal and off-diagonal, from the temporal parameters
+// (p1, p2) of the canonical vector, and their derivatives in p1 (d1) and p2 (d2):
+//   temporal 1 (seperable_spatial_temporal2D.py:186-212): rho = exp(p1),
+//     (1, 1 + rho^2, -rho) / (1 - rho^2); p2 unused;
+//   temporal 2 (seperable_spatial_temporal_idiffusion2D.py:166-189): a = p1,
+//     sigma = exp(p2), (sigma, (1 + a^2) sigma, -a sigma).
+// Returns false when rho >= 1 (Qt would not be positive definite).
+inline bool separable_qt(int temporal, double p1, double p2, double* qt, double* d1 = nullptr,
+                         double* d2 = nullptr) {
+  double e1[3], e2[3];
+  if (temporal == 1) {
+    const double rho = std::exp(p1), r2 = rho * rho, q = 1.0 - r2;
+    if (!(q > 0.0)) return false;
+    qt[0] = 1.0 / q; qt[1] = (1.0 + r2) / q; qt[2] = -rho / q;
+    // rho d/drho
+    e1[0] = 2.0 * r2 / (q * q); e1[1] = 4.0 * r2 / (q * q); e1[2] = -rho * (1.0 + r2) / (q * q);
+    e2[0] = e2[1] = e2[2] = 0.0;
+  } else {
+    const double a = p1, sigma = std::exp(p2);
+    qt[0] = sigma; qt[1] = (1.0 + a * a) * sigma; qt[2] = -a * sigma;
+    e1[0] = 0.0; e1[1] = 2.0 * a * sigma; e1[2] = -sigma;
+    e2[0] = qt[0]; e2[1] = qt[1]; e2[2] = qt[2];
+  }
+  for (int i = 0; i < 3; ++i) {
+    if (d1) d1[i] = e1[i];
+    if (d2) d2[i] = e2[i];
+  }
+  return true;
+}
+
+// The spatial operator of a separable model: its model description as T == 1.
+inline DevModel spatial_view(const DevModel& m) {
+  DevModel s = m;
+  s.T = 1;
+  s.adv = 0;
+  s.nw = 0;
+  return s;
+}
+
 struct Plan {
   Symbolic sym;
   int precision = 1;  // 0: FP64 throughout ("plain"); 1: FP32 factor, FP64 pivots/refinement ("mixed")
@@ -102,6 +143,10 @@ struct Plan {
   double *d_Q0 = nullptr, *d_QA = nullptr, *d_QO = nullptr, *d_cQs = nullptr;
   bool assembled = false;
   double cfac = 1.0;
+  // separable models (sym.nslots == kSlotsSep): Qt end / interior diagonal and
+  // off-diagonal, and the temporal parametrisation (1: log rho, 2: a, log sigma)
+  int temporal = 0;
+  double qt[3] = {0.0, 0.0, 0.0};
   std::vector<double> theta;
   // observations
   int* d_obs_cnt = nullptr;   // per natural node
@@ -145,6 +190,8 @@ struct Plan {
     QStencil q;
     q.Q0 = d_Q0; q.QA = d_QA; q.QO = d_QO; q.cQs = d_cQs;
     q.Mx = sym.Mx; q.Ny = sym.Ny; q.T = sym.T; q.Ns = sym.Mx * sym.Ny;
+    q.sep = sym.nslots == kSlotsSep ? 1 : 0;
+    q.qt_end = qt[0]; q.qt_mid = qt[1]; q.qt_off = qt[2];
     return q;
   }
   size_t esize() const { return precision == 0 ? sizeof(double) : sizeof(float); }

@@ -12,9 +12,13 @@
 namespace spde {
 
 // Stencil slots of one node: dt = -1 (9), dt = 0 (25), dt = +1 (9); T == 1 keeps
-// only the 25 same-slice slots.
+// only the 25 same-slice slots.  Separable space-time models (Q = Qt (x) Qs,
+// spdes/seperable_spatial_temporal2D.py:64-83) couple |dx|,|dy| <= 2 in the
+// neighbouring slices too: 3 x 25 slots, slot = (dt + 1) 25 + (dy + 2) 5 + dx + 2.
+// The slot count identifies the layout.
 constexpr int kSlotsST = 43;
 constexpr int kSlotsS = 25;
+constexpr int kSlotsSep = 75;
 
 struct Front {
   int parent = -1;
@@ -62,11 +66,12 @@ struct Symbolic {
   double nnz_l = 0.0;           // entries of L (lower, dense fronts)
 };
 
-// Stencil offset table: slot -> (dx, dy, dt).
-void slot_offsets(int T, int* dx, int* dy, int* dt);
+// Stencil offset table of a layout with `nslots` slots: slot -> (dx, dy, dt).
+void slot_offsets(int nslots, int* dx, int* dy, int* dt);
 
 // Build the symbolic analysis for an Mx x Ny x T lattice.  `leaf_max` bounds the
-// node count of an undivided box; `nbk` is the diagonal block size.
-int build_symbolic(int Mx, int Ny, int T, int leaf_max, int nbk, Symbolic* out);
+// node count of an undivided box; `nbk` is the diagonal block size; `separable`
+// selects the 75-slot layout (T >= 2).
+int build_symbolic(int Mx, int Ny, int T, int leaf_max, int nbk, Symbolic* out, bool separable = false);
 
 }  // namespace spde

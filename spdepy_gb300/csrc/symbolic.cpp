@@ -19,15 +19,21 @@
 
 namespace spde {
 
-void slot_offsets(int T, int* dx, int* dy, int* dt) {
+void slot_offsets(int nslots, int* dx, int* dy, int* dt) {
   int s = 0;
-  if (T > 1) {
+  if (nslots == kSlotsSep) {
+    for (int c = -1; c <= 1; ++c)
+      for (int a = -2; a <= 2; ++a)
+        for (int b = -2; b <= 2; ++b) { dx[s] = b; dy[s] = a; dt[s] = c; ++s; }
+    return;
+  }
+  if (nslots == kSlotsST) {
     for (int a = -1; a <= 1; ++a)
       for (int b = -1; b <= 1; ++b) { dx[s] = b; dy[s] = a; dt[s] = -1; ++s; }
   }
   for (int a = -2; a <= 2; ++a)
     for (int b = -2; b <= 2; ++b) { dx[s] = b; dy[s] = a; dt[s] = 0; ++s; }
-  if (T > 1) {
+  if (nslots == kSlotsST) {
     for (int a = -1; a <= 1; ++a)
       for (int b = -1; b <= 1; ++b) { dx[s] = b; dy[s] = a; dt[s] = 1; ++s; }
   }
@@ -40,6 +46,7 @@ inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 struct NDBuilder {
   Symbolic* S;
   int Mx, Ny, T, leaf_max;
+  int rt = 1;  // spatial reach of the coupling to the neighbouring time slices
   int next_new = 0;
 
   inline int nat(int x, int y, int t) const { return (t * Ny + y) * Mx + x; }
@@ -111,8 +118,8 @@ struct NDBuilder {
           if (!inside) out.push_back(S->perm[nat(x, y, t)]);
         }
     if (T > 1) {
-      int xa1 = std::max(0, b[0] - 1), xb1 = std::min(Mx, b[1] + 1);
-      int ya1 = std::max(0, b[2] - 1), yb1 = std::min(Ny, b[3] + 1);
+      int xa1 = std::max(0, b[0] - rt), xb1 = std::min(Mx, b[1] + rt);
+      int ya1 = std::max(0, b[2] - rt), yb1 = std::min(Ny, b[3] + rt);
       for (int t : {b[4] - 1, b[5]}) {
         if (t < 0 || t >= T) continue;
         for (int y = ya1; y < yb1; ++y)
@@ -135,18 +142,19 @@ int front_pos(const Symbolic& S, const Front& f, int v) {
 
 }  // namespace
 
-int build_symbolic(int Mx, int Ny, int T, int leaf_max, int nbk, Symbolic* out) {
-  if (Mx < 1 || Ny < 1 || T < 1 || leaf_max < 1 || nbk < 8) return -1;
+int build_symbolic(int Mx, int Ny, int T, int leaf_max, int nbk, Symbolic* out, bool separable) {
+  if (Mx < 1 || Ny < 1 || T < 1 || leaf_max < 1 || nbk < 8 || (separable && T < 2)) return -1;
   Symbolic& S = *out;
   S = Symbolic();
   S.Mx = Mx; S.Ny = Ny; S.T = T;
   int64_t n64 = int64_t(Mx) * Ny * T;
   if (n64 > INT32_MAX / 64) return -2;
   S.n = int(n64);
-  S.nslots = T > 1 ? kSlotsST : kSlotsS;
+  S.nslots = separable ? kSlotsSep : (T > 1 ? kSlotsST : kSlotsS);
   S.nbk = nbk;
   S.perm.assign(S.n, -1);
   NDBuilder B{&S, Mx, Ny, T, leaf_max};
+  B.rt = separable ? 2 : 1;
   int root[6] = {0, Mx, 0, Ny, 0, T};
   B.build(root, 0);
   if (B.next_new != S.n) return -3;
@@ -219,7 +227,7 @@ int build_symbolic(int Mx, int Ny, int T, int leaf_max, int nbk, Symbolic* out) 
   S.dinv_size = doff;
   // assembly map: (natural node, slot) -> offset in its front panel
   std::vector<int> dx(S.nslots), dy(S.nslots), dt(S.nslots);
-  slot_offsets(T, dx.data(), dy.data(), dt.data());
+  slot_offsets(S.nslots, dx.data(), dy.data(), dt.data());
   S.amap.assign(int64_t(S.n) * S.nslots, -1);
   for (int t = 0; t < T; ++t)
     for (int y = 0; y < Ny; ++y)

@@ -91,13 +91,14 @@ class Layout:
 class GPUPlan:
     """Owns one native plan (symbolic analysis + device arenas) for a grid."""
 
-    def __init__(self, grid: Grid, precision="mixed", leaf_max=128):
+    def __init__(self, grid: Grid, precision="mixed", leaf_max=128, separable=False):
         self.grid = grid
         self.precision = precision
         self._h = ctypes.c_void_p()
-        nat.check(nat.lib().spde_plan_create(grid.Mx, grid.Ny, grid.T, PRECISION[precision], leaf_max,
-                                             ctypes.byref(self._h)), what="plan")
-        self.nslots = 25 if grid.T == 1 else 43
+        create = nat.lib().spde_plan_create_separable if separable else nat.lib().spde_plan_create
+        nat.check(create(grid.Mx, grid.Ny, grid.T, PRECISION[precision], leaf_max, ctypes.byref(self._h)),
+                  what="plan")
+        self.nslots = 75 if separable else (25 if grid.T == 1 else 43)
         self.layout = None
         self._obs = None
         self._akey = None   # parameters of the assembled model
@@ -120,7 +121,7 @@ class GPUPlan:
         nat.check(nat.lib().spde_plan_info(self._h, ctypes.byref(info)), self._h)
         return info
 
-    def set_model(self, layout: Layout, bc, mod0_diff, mod0_bc, ww=None):
+    def set_model(self, layout: Layout, bc, mod0_diff, mod0_bc, ww=None, temporal=0):
         g = self.grid
         self._keep = []
 
@@ -134,7 +135,7 @@ class GPUPlan:
         d = nat.ModelDesc(g.Mx, g.Ny, g.T, bc, g.hx, g.hy, g.dt, DIFF_CODE[layout.diff], int(layout.var_h),
                           ADV_CODE[layout.adv], layout.nbasis, arr(g.bs if layout.var_h else None),
                           arr(g.bsH if layout.var_h else None), arr(g.bsA if layout.adv == "v" else None),
-                          arr(ww if layout.adv == "cov" else None), DIFF_CODE[mod0_diff], mod0_bc)
+                          arr(ww if layout.adv == "cov" else None), DIFF_CODE[mod0_diff], mod0_bc, temporal)
         nat.check(nat.lib().spde_set_model(self._h, ctypes.byref(d)), self._h, "set_model")
         self.layout = layout
         self._keep = []
@@ -300,7 +301,11 @@ class PrecisionQ:
         return stencil_to_csr(self.spde.grid, qv)
 
 
-def stencil_offsets(T):
+def stencil_offsets(T, nslots=None):
+    """(dx, dy, dt) of every slot of the 25 (spatial), 43 (spatio-temporal) or 75
+    (separable) slot layout."""
+    if nslots == 75:
+        return [(dx, dy, dt) for dt in range(-1, 2) for dy in range(-2, 3) for dx in range(-2, 3)]
     if T == 1:
         return [(dx, dy, 0) for dy in range(-2, 3) for dx in range(-2, 3)]
     out = [(dx, dy, -1) for dy in range(-1, 2) for dx in range(-1, 2)]
@@ -317,7 +322,7 @@ def stencil_to_csr(grid, qv):
     t, r = np.divmod(k, Mx * Ny)
     y, x = np.divmod(r, Mx)
     rows, cols, vals = [], [], []
-    for s, (dx, dy, dt) in enumerate(stencil_offsets(T)):
+    for s, (dx, dy, dt) in enumerate(stencil_offsets(T, qv.shape[1])):
         ok = (x + dx >= 0) & (x + dx < Mx) & (y + dy >= 0) & (y + dy < Ny) & (t + dt >= 0) & (t + dt < T)
         rows.append(k[ok])
         cols.append(((t + dt) * Ny + y + dy)[ok] * Mx + (x + dx)[ok])
@@ -668,11 +673,142 @@ for _fam, _names in _NAMES.items():
         globals()[_nm] = _CLASSES[(_fam, _d)]
 
 
+class SeparableModel(SpdeModel):
+    """Separable space-time model Q = Qt (x) Qs (reference
+    spdes/seperable_spatial_temporal{,_ha,_idiffusion}2D.py).
+
+    Qs = A^T V^-1 A with A = V kappa - A_H is the spatially varying Whittle-Matern
+    operator (B-spline kappa, gamma and, unless isotropic, vx, vy); Qt is the
+    tridiagonal AR(1) precision over the T steps: in log rho for the anisotropic
+    class (parameters kappa, gamma, vx, vy, log rho, log tau), in (a, log sigma)
+    for the isotropic and half-angle classes (kappa, gamma, [vx, vy,] a,
+    log sigma, log tau).  The GPU plan uses the 75-slot separable stencil."""
+
+    family = "seperable-spatial-temporal"
+    diff = "ani"
+
+    def __init__(self, grid, par=None, bc=3, precision="mixed", **_):
+        if grid.T < 2:
+            raise ValueError("separable space-time models need a grid with t")
+        self.grid = grid
+        self.bc = int(bc)
+        if self.bc not in (1, 3):
+            raise ValueError("bc must be 1 (Neumann) or 3 (Dirichlet); periodic bc=2 is not supported")
+        self.layout = Layout("var-whittle-matern", self.diff, grid.Nbs2)
+        self.temporal = 1 if self.diff == "ani" else 2
+        self.nspat = self.layout.nself
+        self.layout.nself = self.nspat + (1 if self.temporal == 1 else 2)
+        self.layout.nbase = self.layout.nself + 1
+        if self.temporal == 1:
+            self.layout.sl["rho"] = slice(self.nspat, self.nspat + 1)
+        else:
+            self.layout.sl["a"] = slice(self.nspat, self.nspat + 1)
+            self.layout.sl["sigma"] = slice(self.nspat + 1, self.nspat + 2)
+        self.type = f"seperable-spatial-temporal-{self.diff}-2D-bc{self.bc}"
+        self.mod0 = None
+        self.ww = None
+        self.precision = precision
+        self.Q = None
+        self.Q_fac = None
+        self.data = None
+        self.r = None
+        self.S = None
+        self.idx = None
+        self._plan = None
+        self._model_key = None
+        self.fitQ0 = False
+        self.par = self.defaults()
+        if par is not None:
+            self.setQ(par=par)
+
+    def defaults(self):
+        """The reference's initFit start vector (seperable_spatial_temporal2D.py:39-41 and the
+        _ha / _idiffusion classes)."""
+        nb = self.grid.Nbs2
+        sp = [np.full(nb, -1.0), np.full(nb, -1.0)]
+        if self.diff != "iso":
+            sp += [np.full(nb, 0.1), np.full(nb, 0.1)]
+        tp = [-1.0] if self.temporal == 1 else [0.1, 1.0]
+        return np.hstack(sp + [tp, [np.log(100.0)]])
+
+    @property
+    def plan(self) -> GPUPlan:
+        if self._plan is None or self._plan.grid is not self.grid:
+            self._plan = GPUPlan(self.grid, self.precision, separable=True)
+            self._model_key = None
+        return self._plan
+
+    def setPars(self, par):
+        self.par = np.asarray(par, dtype=np.float64).copy()
+
+    def getPars(self, onlySelf=True):
+        return self.par.copy()
+
+    def canonical(self, par):
+        par = np.asarray(par, dtype=np.float64)
+        lay, nk = self.layout, self.layout.nk
+        c = np.zeros(lay.ncanon)
+        c[0:nk] = par[lay.sl["kappa"]]
+        c[nk:2 * nk] = par[lay.sl["gamma"]]
+        if "vx" in lay.sl:
+            c[2 * nk:3 * nk] = par[lay.sl["vx"]]
+            c[3 * nk:4 * nk] = par[lay.sl["vy"]]
+        o = 4 * nk
+        c[o] = par[self.nspat]
+        if self.temporal == 2:
+            c[o + 1] = par[self.nspat + 1]
+        c[-1] = par[-1]
+        return c
+
+    def from_canonical_grad(self, gc, par):
+        lay, nk = self.layout, self.layout.nk
+        g = np.zeros(np.asarray(par).size)
+        g[lay.sl["kappa"]] = gc[0:nk]
+        g[lay.sl["gamma"]] = gc[nk:2 * nk]
+        if "vx" in lay.sl:
+            g[lay.sl["vx"]] = gc[2 * nk:3 * nk]
+            g[lay.sl["vy"]] = gc[3 * nk:4 * nk]
+        o = 4 * nk
+        g[self.nspat] = gc[o]
+        if self.temporal == 2:
+            g[self.nspat + 1] = gc[o + 1]
+        g[-1] = gc[-1]
+        return g
+
+    def _ensure_model(self):
+        key = (self.family, self.diff, self.bc)
+        if self._model_key != key:
+            self.plan.set_model(self.layout, self.bc, self.diff, self.bc, None, temporal=self.temporal)
+            self._model_key = key
+
+    def initFit(self, data, **kwargs):
+        """Attach data and the observation index; returns the reference's start
+        vector (seperable_spatial_temporal2D.py:39-49)."""
+        data = np.asarray(data, dtype=np.float64)
+        assert data.shape[0] <= self.grid.n
+        self.data = data
+        self.r = data.shape[1] if data.ndim == 2 else 1
+        self.idx = kwargs.get("idx")
+        self.S = self.grid.getS(self.idx)
+        self._y_pinned = None
+        return self.defaults()
+
+
+SeperableSpatialTemporal2D = type("SeperableSpatialTemporal2D", (SeparableModel,), {"diff": "ani"})
+SeperableSpatialTemporalHa2D = type("SeperableSpatialTemporalHa2D", (SeparableModel,), {"diff": "ha"})
+SeperableSpatialTemporalIDiffusion2D = type("SeperableSpatialTemporalIDiffusion2D", (SeparableModel,),
+                                            {"diff": "iso"})
+
+
 def spde_init(model, grid, parameters=None, ani=True, ha=True, bc=3, mod0=None, ww=None, precision="mixed"):
     """Model factory with the reference's dispatch (spdes/__init__.py:1-184)."""
     name = MODEL_IDS.get(model, model) if not isinstance(model, str) else model
     if name == "seperable-spatial-temporal":
-        raise NotImplementedError("separable space-time models are not on the GPU path")
+        if grid.T == 1:
+            raise ValueError("separable space-time models need a grid with t")
+        cls = (SeperableSpatialTemporalHa2D if ha else
+               SeperableSpatialTemporal2D if ani else SeperableSpatialTemporalIDiffusion2D)
+        return cls(grid=grid, par=parameters, bc=bc, precision=precision)
     if name not in FAMILIES:
         raise ValueError(f"unknown model {model!r}")
     diff = "ha" if ha else ("ani" if ani else "iso")
