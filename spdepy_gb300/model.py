@@ -155,7 +155,7 @@ class Model:
             raise NotImplementedError("marginal variances with fixed effects are not on the GPU path")
         self._factor_current()
         zq = self.mod.plan.selinv()
-        centre = 12 if self.grid.T == 1 else 21
+        centre = self.mod.plan.nslots // 2  # the (0, 0, 0) slot of every stencil layout
         self.mvar = zq[:, centre].cpu().numpy()
         return self.mvar
 
