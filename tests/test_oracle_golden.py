@@ -176,3 +176,34 @@ def test_fixed_effect_draws_have_the_augmented_covariance():
     G = np.vstack([xn, xb])  # x = G z
     Qaug = np.block([[A, border.B], [border.B.T, border.C]])
     assert np.allclose(G @ G.T, np.linalg.inv(Qaug), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", separable_cases())
+def test_separable_host_mapping(name):
+    """Host side of the separable GPU models (no device needed): the reference's
+    dispatch, the parameter vector <-> canonical vector round trip, the default
+    start vector and the 75-slot stencil export against the oracle's Q."""
+    from golden_cases import diff_form, grid_args
+    from spdepy_gb300.grids import Grid
+    from spdepy_gb300.spdes import SeparableModel, spde_init, stencil_offsets, stencil_to_csr
+    g = load(name)
+    ga = grid_args(g)
+    grid = Grid(ga["x"], ga["y"], ga["t"], ga["extend"], ga["Nbs"])
+    d = diff_form(g)
+    mod = spde_init("seperable-spatial-temporal", grid, ani=d != "iso", ha=d == "ha", bc=int(g["bc"]))
+    assert isinstance(mod, SeparableModel) and mod.diff == d
+    par = np.asarray(g["par"], float)
+    assert mod.initFit(g["y"], idx=g["idx"]).size == par.size
+    c = mod.canonical(par)
+    assert c.size == mod.layout.ncanon
+    assert np.array_equal(mod.from_canonical_grad(c, par), par)
+    Q = separable_oracle(g).makeQ(par).tocsr()
+    n, Mx, Ny, T = Q.shape[0], grid.Mx, grid.Ny, grid.T
+    k = np.arange(n)
+    t, r = np.divmod(k, Mx * Ny)
+    y, x = np.divmod(r, Mx)
+    qv = np.zeros((n, 75))
+    for s, (dx, dy, dt) in enumerate(stencil_offsets(T, 75)):
+        ok = (x + dx >= 0) & (x + dx < Mx) & (y + dy >= 0) & (y + dy < Ny) & (t + dt >= 0) & (t + dt < T)
+        qv[ok, s] = np.asarray(Q[k[ok], (((t + dt) * Ny + y + dy) * Mx + x + dx)[ok]]).ravel()
+    assert abs(stencil_to_csr(grid, qv) - Q).max() == 0.0
