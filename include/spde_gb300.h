@@ -149,6 +149,13 @@ int spde_spmv(SpdePlan* plan, int with_obs, double tau, const double* x_dev, dou
 /* ---- observations: S = selected identity rows (grids/spat2Dtemp_regular_mesh.py:35-58);
  * idx are node indices (duplicates allowed), host int64. */
 int spde_set_obs(SpdePlan* plan, const int64_t* idx_host, int m);
+/* The same with a weight per observation (host FP64, finite, >= 0): the
+ * matrices "with observations" become Q + tau sum_i w_i e_{idx_i} e_{idx_i}^T.
+ * Model.update accumulates Q += tau_k S_k^T S_k over calls whose tau_k differ
+ * (model.py:120-127): weights tau_k with tau = 1 give that sum.  spde_loglike
+ * and the conditional-mean right-hand sides treat every observation alike and
+ * are meant for unweighted sets. */
+int spde_set_obs_weighted(SpdePlan* plan, const int64_t* idx_host, const double* weights_host, int m);
 
 /* ---- factorisation: cholesky(Q) / cholesky(Q + tau S^T S) and Factor.logdet()
  * (spdes/advection_diffusion2D.py:117,192-193,198). */
@@ -179,7 +186,11 @@ int spde_adjoint(SpdePlan* plan, const double* gbar_dev, double* grad_host);
  * SPDE_ERR_ARG).  The first call on a device looks up that array's device
  * address (cudaGetSymbolAddress); make that first call before any stream
  * capture.  All calls share the one array: calls that overlap on the GPU
- * (other streams, other host threads, other plans) race on it. */
+ * (other streams, other host threads, other plans) race on it.  Unlike
+ * spde_adjoint, the call only enqueues the work on the plan's stream (on the
+ * plan's device, whichever device is current) and returns before the gradient
+ * is written: gbar_dev must be ready on that stream, and grad_dev is valid once
+ * the stream has reached this point (e.g. after cudaStreamSynchronize). */
 int spde_adjoint_noalloc(SpdePlan* plan, const double* gbar_dev, double* grad_dev);
 
 /* ---- log-likelihood and gradient: logLike (spdes/advection_diffusion2D.py:187-223).

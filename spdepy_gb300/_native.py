@@ -67,6 +67,7 @@ SIGNATURES = {
     "spde_export_q": (_I, [_P, _I, _D, _P]),
     "spde_spmv": (_I, [_P, _I, _D, _P, _P, _I]),
     "spde_set_obs": (_I, [_P, _P, _I]),
+    "spde_set_obs_weighted": (_I, [_P, _P, _P, _I]),
     "spde_factor": (_I, [_P, _I, _D, ctypes.POINTER(_D)]),
     "spde_solve": (_I, [_P, _P, _P, _I, _I, _D, ctypes.POINTER(_D)]),
     "spde_sample": (_I, [_P, _P, _P, _I]),

@@ -342,7 +342,8 @@ __global__ void coef_reduce_kernel(DevModel m, const double* __restrict__ cg, do
   }
 }
 
-int64_t adjoint_work_elems(const Plan* p) { return int64_t(p->sym.Mx) * p->sym.Ny * (84 + kCW); }
+int64_t adjoint_work_elems(const Plan* p) { return int64_t(p->sym.Mx) * p->sym.Ny * kAdjointCellElems; }
+static_assert(kAdjointCellElems == 84 + kCW, "adjoint work per cell: 84 reduced stencil values + kCW partials");
 
 // ---------------------------------------------------------------------------
 // Fixed scratch of the allocation-free adjoint entry point (spde_adjoint_noalloc).
@@ -353,15 +354,20 @@ int64_t adjoint_work_elems(const Plan* p) { return int64_t(p->sym.Mx) * p->sym.N
 constexpr int64_t kNoAllocElems = int64_t(1) << 20;  // doubles
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocElems];
 
-int noalloc_scratch(double** ptr, int64_t* elems) {
+int noalloc_scratch(int dev, double** ptr, int64_t* elems) {
   static std::mutex mu;
   static double* cache[64] = {nullptr};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  if (dev < 0 || dev >= 64) return 1;
   std::lock_guard<std::mutex> lock(mu);
   if (!cache[dev]) {
+    // the lookup must run with `dev` current: switch to it and back
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) return 1;
+    if (cur != dev && cudaSetDevice(dev) != cudaSuccess) return 1;
     void* addr = nullptr;
-    if (cudaGetSymbolAddress(&addr, g_noalloc_scratch) != cudaSuccess || !addr) return 1;
+    const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (cur != dev) cudaSetDevice(cur);
+    if (e != cudaSuccess || !addr) return 1;
     cache[dev] = static_cast<double*>(addr);
   }
   *ptr = cache[dev];

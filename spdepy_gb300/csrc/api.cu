@@ -349,6 +349,7 @@ static int plan_create(int Mx, int Ny, int T, int precision, int leaf_max, bool 
   SpdePlan* plan = new (std::nothrow) SpdePlan();
   if (!plan) return SPDE_ERR_NO_MEMORY;
   plan->p.precision = precision;
+  if (cudaGetDevice(&plan->p.device) != cudaSuccess) plan->p.device = 0;
   if (precision == SPDE_PRECISION_ITERATIVE) {
     // assembly, products and iterative solves only: no ordering, no factor arenas
     if (Mx < 3 || Ny < 3 || T < 1 || int64_t(Mx) * Ny * T > (int64_t(1) << 31) - 1) {
@@ -593,24 +594,39 @@ int spde_spmv(SpdePlan* plan, int with_obs, double tau, const double* x, double*
   return SPDE_OK;
 }
 
-int spde_set_obs(SpdePlan* plan, const int64_t* idx, int m) {
+// Observation set with per-observation weights (nullptr: 1 each): node k's
+// weight is the sum over the observations at k, so tau * weight is what
+// tau S^T S adds to Q's diagonal.
+static int set_obs(SpdePlan* plan, const int64_t* idx, const double* wts, int m) {
   if (!plan || (m > 0 && !idx) || m < 0) return SPDE_ERR_ARG;
   Plan& p = plan->p;
-  std::vector<int> cnt(p.sym.n, 0), id(std::max(m, 1), 0);
+  std::vector<double> cnt(p.sym.n, 0.0);
+  std::vector<int> id(std::max(m, 1), 0);
   for (int i = 0; i < m; ++i) {
     if (idx[i] < 0 || idx[i] >= p.sym.n) { p.last_error = "observation index out of range"; return SPDE_ERR_ARG; }
-    cnt[idx[i]] += 1;
+    if (wts && !(std::isfinite(wts[i]) && wts[i] >= 0.0)) {
+      p.last_error = "observation weights must be finite and non-negative";
+      return SPDE_ERR_ARG;
+    }
+    cnt[idx[i]] += wts ? wts[i] : 1.0;
     id[i] = int(idx[i]);
   }
   cudaFree(p.d_obs_cnt); cudaFree(p.d_obs_idx);
   p.d_obs_cnt = nullptr; p.d_obs_idx = nullptr;
-  API_CUDA(cudaMalloc(&p.d_obs_cnt, cnt.size() * sizeof(int)));
+  API_CUDA(cudaMalloc(&p.d_obs_cnt, cnt.size() * sizeof(double)));
   API_CUDA(cudaMalloc(&p.d_obs_idx, id.size() * sizeof(int)));
-  API_CUDA(cudaMemcpy(p.d_obs_cnt, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice));
+  API_CUDA(cudaMemcpy(p.d_obs_cnt, cnt.data(), cnt.size() * sizeof(double), cudaMemcpyHostToDevice));
   API_CUDA(cudaMemcpy(p.d_obs_idx, id.data(), id.size() * sizeof(int), cudaMemcpyHostToDevice));
   p.nobs = m;
   if (p.factored == 2) p.factored = 0;
   return SPDE_OK;
+}
+
+int spde_set_obs(SpdePlan* plan, const int64_t* idx, int m) { return set_obs(plan, idx, nullptr, m); }
+
+int spde_set_obs_weighted(SpdePlan* plan, const int64_t* idx, const double* weights, int m) {
+  if (!weights && m > 0) return SPDE_ERR_ARG;
+  return set_obs(plan, idx, weights, m);
 }
 
 int spde_factor(SpdePlan* plan, int with_obs, double tau, double* logdet) {
@@ -660,13 +676,29 @@ int spde_adjoint_noalloc(SpdePlan* plan, const double* gbar, double* grad_dev) {
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   double* scratch = nullptr;
   int64_t cap = 0;
-  if (noalloc_scratch(&scratch, &cap)) { p.last_error = "fixed scratch not reachable on this device"; return SPDE_ERR_CUDA; }
+  // the plan's own device's copy of the array, whichever device is current
+  if (noalloc_scratch(p.device, &scratch, &cap)) {
+    p.last_error = "fixed scratch not reachable on the plan's device";
+    return SPDE_ERR_CUDA;
+  }
   const int64_t need = adjoint_work_elems(&p);
   if (need > cap) {
     p.last_error = "grid too large for the fixed adjoint scratch (needs " + std::to_string(need) +
-                   " doubles, limit " + std::to_string(cap) + ", i.e. Mx*Ny <= " + std::to_string(cap / 106) + ")";
+                   " doubles, limit " + std::to_string(cap) + ", i.e. Mx*Ny <= " +
+                   std::to_string(cap / kAdjointCellElems) + ")";
     return SPDE_ERR_ARG;
   }
+  // enqueue on the plan's device (its array, its stream), then restore the caller's
+  struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+      if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+      else prev = -1;
+    }
+    ~DeviceGuard() {
+      if (prev >= 0) cudaSetDevice(prev);
+    }
+  } guard(p.device);
   // the kernels write every scratch entry they later read; clear anyway so no
   // value from an earlier call can leak into this one
   API_CUDA(cudaMemsetAsync(scratch, 0, size_t(need) * sizeof(double), p.stream));

@@ -164,7 +164,7 @@ __global__ void qstencil_kernel(DevModel m, const double* __restrict__ Ageo, con
 }
 
 // Q in stencil layout (natural order, nslots values per node), FP64.
-__global__ void qexport_kernel(QStencil q, int nslots, const int* __restrict__ obs_cnt, double tau,
+__global__ void qexport_kernel(QStencil q, int nslots, const double* __restrict__ obs_cnt, double tau,
                                double* __restrict__ out) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t n = int64_t(q.Ns) * q.T;
@@ -186,7 +186,7 @@ __global__ void qexport_kernel(QStencil q, int nslots, const int* __restrict__ o
 template <typename T>
 __global__ void scatter_kernel(QStencil q, int nslots, const int* __restrict__ amap, const int* __restrict__ perm,
                                const int* __restrict__ front_of, const DevFront* __restrict__ fronts,
-                               const int* __restrict__ obs_cnt, double tau, T* __restrict__ L) {
+                               const double* __restrict__ obs_cnt, double tau, T* __restrict__ L) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t n = int64_t(q.Ns) * q.T;
   if (e >= n * nslots) return;
@@ -270,25 +270,25 @@ void launch_qstencil(const DevModel& m, const double* Ageo, const double* A0geo,
                      double* Q0, double* QA, double* QO, double* cQs, double cfac, cudaStream_t st) {
   qstencil_kernel<<<nblk(m.Ns, 128), 128, 0, st>>>(m, Ageo, A0geo, kap, qs, Q0, QA, QO, cQs, cfac);
 }
-void launch_qexport(const QStencil& q, int nslots, const int* obs, double tau, double* out, cudaStream_t st) {
+void launch_qexport(const QStencil& q, int nslots, const double* obs, double tau, double* out, cudaStream_t st) {
   int64_t tot = int64_t(q.Ns) * q.T * nslots;
   qexport_kernel<<<nblk(tot, 256), 256, 0, st>>>(q, nslots, obs, tau, out);
 }
 template <typename T>
 void launch_scatter(const QStencil& q, int nslots, const int* amap, const int* perm, const int* front_of,
-                    const DevFront* fronts, const int* obs, double tau, T* L, cudaStream_t st) {
+                    const DevFront* fronts, const double* obs, double tau, T* L, cudaStream_t st) {
   int64_t tot = int64_t(q.Ns) * q.T * nslots;
   scatter_kernel<T><<<nblk(tot, 256), 256, 0, st>>>(q, nslots, amap, perm, front_of, fronts, obs, tau, L);
 }
 template void launch_scatter<double>(const QStencil&, int, const int*, const int*, const int*, const DevFront*,
-                                     const int*, double, double*, cudaStream_t);
+                                     const double*, double, double*, cudaStream_t);
 template void launch_scatter<float>(const QStencil&, int, const int*, const int*, const int*, const DevFront*,
-                                    const int*, double, float*, cudaStream_t);
+                                    const double*, double, float*, cudaStream_t);
 // y = (Q + tau S^T S) x with one thread per (spatial cell, column) sweeping the
 // time axis: the cell's time-invariant coefficients (25 in-block values, 9 to
 // t + 1 and the 9 mirrored from the neighbours to t - 1) are loaded once and
 // reused for all T blocks.
-__global__ void __launch_bounds__(128) spmv_cells_kernel(QStencil q, const int* __restrict__ obs, double tau,
+__global__ void __launch_bounds__(128) spmv_cells_kernel(QStencil q, const double* __restrict__ obs, double tau,
                                                          const double* __restrict__ x, double* __restrict__ y,
                                                          int nrhs) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(128) spmv_cells_kernel(QStencil q, const int* 
 // Separable Q = Qt (x) Qs: one thread per spatial cell and right-hand side forms
 // the spatial product u_t = sum_s Qs[c, s] x_t(c + off_s) once per time slice and
 // combines y_t = Qt_tt u_t + Qt_off (u_(t-1) + u_(t+1)).
-__global__ void __launch_bounds__(128) spmv_sep_kernel(QStencil q, const int* __restrict__ obs, double tau,
+__global__ void __launch_bounds__(128) spmv_sep_kernel(QStencil q, const double* __restrict__ obs, double tau,
                                                        const double* __restrict__ x, double* __restrict__ y,
                                                        int nrhs) {
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(128) spmv_sep_kernel(QStencil q, const int* __
   }
 }
 
-void launch_spmv(const QStencil& q, const int* obs, double tau, const double* x, double* y, int nrhs,
+void launch_spmv(const QStencil& q, const double* obs, double tau, const double* x, double* y, int nrhs,
                  cudaStream_t st) {
   const int64_t tot = int64_t(q.Ns) * nrhs;
   if (q.sep) spmv_sep_kernel<<<nblk(tot, 128), 128, 0, st>>>(q, obs, tau, x, y, nrhs);

@@ -75,11 +75,11 @@ __device__ __forceinline__ double qval(const QStencil& q, int c, int t, int dx, 
 void launch_fields(const DevModel& m, double* Ageo, double* A0geo, double* kap, double* qs, cudaStream_t st);
 void launch_qstencil(const DevModel& m, const double* Ageo, const double* A0geo, const double* kap, const double* qs,
                      double* Q0, double* QA, double* QO, double* cQs, double cfac, cudaStream_t st);
-void launch_qexport(const QStencil& q, int nslots, const int* obs, double tau, double* out, cudaStream_t st);
+void launch_qexport(const QStencil& q, int nslots, const double* obs, double tau, double* out, cudaStream_t st);
 template <typename T>
 void launch_scatter(const QStencil& q, int nslots, const int* amap, const int* perm, const int* front_of,
-                    const DevFront* fronts, const int* obs, double tau, T* L, cudaStream_t st);
-void launch_spmv(const QStencil& q, const int* obs, double tau, const double* x, double* y, int nrhs,
+                    const DevFront* fronts, const double* obs, double tau, T* L, cudaStream_t st);
+void launch_spmv(const QStencil& q, const double* obs, double tau, const double* x, double* y, int nrhs,
                  cudaStream_t st);
 void launch_diffusion_triplets(int M, int N, const double* H, int field, double hx, double hy, int bc, int* row,
                                int* col, double* val, cudaStream_t st);

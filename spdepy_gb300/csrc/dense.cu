@@ -348,11 +348,11 @@ __global__ void __launch_bounds__(256) panel64_kernel(const GemmTask* __restrict
 
 template <int MODE>
 static void panel64_launch(const GemmTask* t, int n, const float* A, const float* B, float* C, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {  // once, thread-safely (two pipelines launch from two host threads)
     cudaFuncSetAttribute(panel64_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, kPanelSmem);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   panel64_kernel<MODE><<<n, 256, kPanelSmem, st>>>(t, A, B, C);
 }
 

@@ -1055,7 +1055,7 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
   cudaStream_t st = p->stream;
   if (ensure_solve_buffers(p, nrhs)) return 2;
   if (ensure_refine_buffers(p, ne)) return 2;
-  const int* obs = p->factored == 2 ? p->d_obs_cnt : nullptr;
+  const double* obs = p->factored == 2 ? p->d_obs_cnt : nullptr;
   const double tau = p->factored_tau;
   // first solve straight from b
   launch_to_new<T>(b, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);

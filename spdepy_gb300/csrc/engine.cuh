@@ -118,6 +118,7 @@ inline DevModel spatial_view(const DevModel& m) {
 
 struct Plan {
   Symbolic sym;
+  int device = 0;     // CUDA device current when the plan was created
   int precision = 1;  // 0: FP64 throughout ("plain"); 1: FP32 factor, FP64 pivots/refinement ("mixed")
   int tile_m = 64, tile_n = 64;
   cudaStream_t stream = nullptr;
@@ -149,7 +150,7 @@ struct Plan {
   double qt[3] = {0.0, 0.0, 0.0};
   std::vector<double> theta;
   // observations
-  int* d_obs_cnt = nullptr;   // per natural node
+  double* d_obs_cnt = nullptr;  // per natural node: summed observation weights (the count when unweighted)
   int* d_obs_idx = nullptr;   // observed natural nodes (m)
   int nobs = 0;
   // factor state
@@ -218,7 +219,11 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
 
 // adjoint (adjoint.cu)
 void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st);
+// doubles of adjoint work per spatial cell: 84 reduced stencil values + 22 partials
+constexpr int64_t kAdjointCellElems = 106;
 int64_t adjoint_work_elems(const Plan* p);
-int noalloc_scratch(double** ptr, int64_t* elems);
+// device address and size of the allocation-free adjoint's static scratch on
+// device `dev` (looked up once per device with that device current)
+int noalloc_scratch(int dev, double** ptr, int64_t* elems);
 
 }  // namespace spde

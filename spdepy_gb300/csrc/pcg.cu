@@ -53,7 +53,7 @@ __device__ __forceinline__ bool inside(const QStencil& q, int x, int y, int t) {
 }
 
 // Features, network forward and G weights, one thread per node.
-__global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const int* __restrict__ obs, double tau,
+__global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const double* __restrict__ obs, double tau,
                                                          const float* __restrict__ prm, float* __restrict__ w,
                                                          float* __restrict__ act) {
   __shared__ float sp[kNP];
@@ -154,7 +154,7 @@ __global__ void pc_to_f32_kernel(const double* __restrict__ x, float* __restrict
 }
 
 // Jacobi: out = x / A_pp
-__global__ void pc_jacobi_kernel(QStencil q, const int* __restrict__ obs, double tau, const double* __restrict__ x,
+__global__ void pc_jacobi_kernel(QStencil q, const double* __restrict__ obs, double tau, const double* __restrict__ x,
                                  double* __restrict__ out, int nrhs) {
   const int n = q.Ns * q.T;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -353,7 +353,7 @@ __global__ void pcg_p_kernel(double* __restrict__ p, const double* __restrict__ 
 }
 
 // z -= omega D^-1 (A z) for one damped-Jacobi sweep (az = A z)
-__global__ void jacobi_sweep_kernel(QStencil q, const int* __restrict__ obs, double tau, double omega,
+__global__ void jacobi_sweep_kernel(QStencil q, const double* __restrict__ obs, double tau, double omega,
                                     const double* __restrict__ az, double* __restrict__ z, int nrhs) {
   const int64_t n = int64_t(q.Ns) * q.T;
   const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -397,7 +397,7 @@ double* scratch(Plan* p, size_t elems) {
   return static_cast<double*>(p->d_pc);
 }
 
-void apply_precond(Plan* p, int kind, const float* w, const int* obs, double tau, const double* r, double* z,
+void apply_precond(Plan* p, int kind, const float* w, const double* obs, double tau, const double* r, double* z,
                    double* tmp, int nrhs) {
   const QStencil q = p->qstencil();
   const int64_t len = int64_t(p->sym.n) * nrhs;
@@ -510,7 +510,7 @@ int pc_grad(Plan* p, int with_obs, double tau, const float* prm, const float* w,
   float* dout = reinterpret_cast<float*>(sums + 8);
   float* bpart = dout + size_t(n) * kOff;
   const QStencil q = p->qstencil();
-  const int* obs = with_obs ? p->d_obs_cnt : nullptr;
+  const double* obs = with_obs ? p->d_obs_cnt : nullptr;
   cudaStream_t st = p->stream;
   pc_apply_kernel<1, double, double><<<nblk(len), 256, 0, st>>>(q, w, z, y, k);           // y = G^T z
   launch_spmv(q, obs, tau, y, u, k, st);                                   // u = A y
@@ -524,11 +524,11 @@ int pc_grad(Plan* p, int with_obs, double tau, const float* prm, const float* w,
   const double scale = -2.0 / double(len);
   pc_wgrad_kernel<<<nblk(n, 128), 128, 0, st>>>(q, z, e, u, g2, k, scale, act, dout);
   const size_t smem = sizeof(float) * (kHid * kHid + kOff * kHid + kBwNodes * (kFeat + 4 * kHid + kOff));
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [smem] {  // once, thread-safely
     cudaFuncSetAttribute(pc_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   pc_backward_kernel<<<nbw, 128, smem, st>>>(n, prm, act, dout, bpart);
   pc_colsum_kernel<<<nblk(kNP, 128), 128, 0, st>>>(bpart, nbw, grad);
   double h = 0.0;
@@ -551,7 +551,7 @@ int jacobi_smooth(Plan* p, int with_obs, double tau, double omega, int sweeps, d
   if (!base) return 4;
   double *az = base, *part = az + len, *ss = part + size_t(kDotBlocks) * nrhs;
   const QStencil q = p->qstencil();
-  const int* obs = with_obs ? p->d_obs_cnt : nullptr;
+  const double* obs = with_obs ? p->d_obs_cnt : nullptr;
   for (int it = 0; it < sweeps; ++it) {
     launch_spmv(q, obs, tau, z, az, nrhs, p->stream);
     jacobi_sweep_kernel<<<nblk(len), 256, 0, p->stream>>>(q, obs, tau, omega, az, z, nrhs);
@@ -573,7 +573,7 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
   double *rz = sc, *rzn = sc + nrhs, *pap = sc + 2 * nrhs, *rr = sc + 3 * nrhs, *bb = sc + 4 * nrhs;
   int* done = reinterpret_cast<int*>(sc + 8 * nrhs);
   const QStencil q = p->qstencil();
-  const int* obs = with_obs ? p->d_obs_cnt : nullptr;
+  const double* obs = with_obs ? p->d_obs_cnt : nullptr;
   cudaStream_t st = p->stream;
   cudaMemsetAsync(x, 0, size_t(len) * sizeof(double), st);
   cudaMemcpyAsync(r, b, size_t(len) * sizeof(double), cudaMemcpyDeviceToDevice, st);

@@ -386,11 +386,13 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
 
 template <int MODE, int AL, int BL>
 void launch_one(const GemmTask* t, int n, const float* A, const float* B, float* C, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
+  // once per instantiation; a function-local static is initialised thread-safely
+  // (the second log-likelihood pipeline launches from its own host thread)
+  static const bool attr = [] {
     cudaFuncSetAttribute(tc_gemm_kernel<MODE, AL, BL>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   tc_gemm_kernel<MODE, AL, BL><<<n, kThreads, kSmem, st>>>(t, A, B, C);
 }
 

@@ -40,8 +40,7 @@ class Model:
         self.useCov = False
         self.sigmas = np.log(np.array([0.01, 140]))
         self.tau = None
-        self._obs_nodes = np.zeros(0, dtype=np.int64)
-        self._obs_tau = None
+        self._obs = []  # (nodes, tau) of every update since setModel
         self.border = None
 
     def model(self, spde=None, grid=None, parameters=None, ani=True, ha=True, bc=3, mod0=None):
@@ -77,8 +76,7 @@ class Model:
             self.mod.setQ()
         self.Q = self.mod.Q
         self.tau = float(np.exp(self.mod.par[-1]))
-        self._obs_nodes = np.zeros(0, dtype=np.int64)
-        self._obs_tau = None
+        self._obs = []
         self.border = None
         n = self.grid.n
         if not self.useCov:
@@ -104,12 +102,20 @@ class Model:
         self.border = Border(n, np.exp(np.atleast_1d(np.asarray(self.sigmas, float))))
 
     def _factor_current(self):
+        """Factor Q plus the observation terms of every update so far: the
+        reference's self.Q after Q += tau_k S_k^T S_k per call (model.py:122)."""
         plan = self.mod.plan
         self.mod._assemble(self.mod.par)
-        if self._obs_nodes.size:
-            plan.set_obs(self._obs_nodes)
-            return plan.factor(True, self._obs_tau)
-        return plan.factor(False, 0.0)
+        if not self._obs:
+            return plan.factor(False, 0.0)
+        nodes = np.concatenate([nd for nd, _ in self._obs])
+        taus = {t for _, t in self._obs}
+        if len(taus) == 1:
+            plan.set_obs(nodes)
+            return plan.factor(True, taus.pop())
+        # different precisions per call: per-observation weights tau_k, tau = 1
+        plan.set_obs(nodes, weights=np.concatenate([np.full(nd.size, t) for nd, t in self._obs]))
+        return plan.factor(True, 1.0)
 
     def _solve_A(self, R):
         """A^-1 R with the current factor (R: n x k host array)."""
@@ -145,19 +151,50 @@ class Model:
         return data
 
     def qinv(self, simple=False):
-        """Marginal variances diag(Q^-1) (reference model.py:89-118)."""
+        """Marginal variances (reference model.py:89-118), float32 like the
+        reference's.  Without fixed effects: diag(Q^-1) of the current precision
+        (Q plus every update's tau S^T S) from the GPU selected inverse, in place of
+        R-INLA's.  With fixed effects the reference inverts S Q_aug S^T (S =
+        getS() with its fixed-effect columns) and returns its diagonal in an
+        (n + p)-vector; here the same diagonal comes from the selected inverse of A
+        (the lattice block of Q_aug) and a Woodbury correction for the rank-2p
+        border terms."""
         if simple:
             z = self.sample(n=1000, simple=True)
             return z.var(axis=1)
         if self.Q is None:
             self.setModel()
-        if self.useCov:
-            raise NotImplementedError("marginal variances with fixed effects are not on the GPU path")
+        plan = self.mod.plan
+        centre = plan.nslots // 2  # the (0, 0, 0) slot of every stencil layout
         self._factor_current()
-        zq = self.mod.plan.selinv()
-        centre = self.mod.plan.nslots // 2  # the (0, 0, 0) slot of every stencil layout
-        self.mvar = zq[:, centre].cpu().numpy()
+        if self.useCov and self.border is not None:
+            self.mvar = self._qinv_fixed_effects(centre)
+            return self.mvar
+        zq = plan.selinv()
+        self.mvar = zq[:, centre].cpu().numpy().astype(np.float32)
         return self.mvar
+
+    def _qinv_fixed_effects(self, centre):
+        """diag((S Q_aug S^T)^-1) with S = [I | X] and Q_aug = [[A, B], [B^T, C]]:
+        S Q_aug S^T = A + U W U^T, U = [X, B], W = [[C, I], [I, 0]], so with
+        Y = A^-1 U and K = (W^-1 + U^T Y)^-1, W^-1 = [[0, I], [I, -C]]:
+        diag = diag(A^-1) - rowsum((Y K) * Y)."""
+        g = self.grid
+        if g.Ne:
+            raise NotImplementedError("marginal variances with fixed effects on an extended grid: S selects a "
+                                      "principal submatrix of the lattice precision, whose inverse the selected "
+                                      "inverse of the whole lattice does not give")
+        n, p = g.n, self.border.p
+        X = g._fixed_effects()
+        U = np.hstack([X, self.border.B])
+        Y = self._solve_A(U).reshape(n, 2 * p)   # before the selected inversion consumes the factor
+        Winv = np.block([[np.zeros((p, p)), np.eye(p)], [np.eye(p), -self.border.C]])
+        K = np.linalg.inv(Winv + U.T @ Y)
+        zq = self.mod.plan.selinv()
+        d = zq[:, centre].cpu().numpy() - np.einsum("ij,ij->i", Y @ K, Y)
+        mvar = np.zeros(n + p, dtype=np.float32)
+        mvar[:n] = d
+        return mvar
 
     def update(self, y, idx, tau=None):
         """Conditional mean with the observations (reference model.py:120-127)."""
@@ -165,11 +202,8 @@ class Model:
         if self.Q is None:
             self.setModel()
         tau = self.tau if tau is None else float(tau)
-        if self._obs_tau is not None and tau != self._obs_tau:
-            raise NotImplementedError("observations with different precisions in one model")
         nodes = self.grid.obs_nodes(idx)
-        self._obs_nodes = np.concatenate([self._obs_nodes, nodes])
-        self._obs_tau = tau
+        self._obs.append((nodes, tau))
         self._factor_current()
         if self.useCov and self.border is not None:
             rows = np.arange(self.grid.M * self.grid.N * self.grid.T) if idx is None else np.asarray(idx, np.int64)

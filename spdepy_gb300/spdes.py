@@ -140,12 +140,22 @@ class GPUPlan:
         self.layout = layout
         self._keep = []
 
-    def set_obs(self, nodes):
+    def set_obs(self, nodes, weights=None):
+        """Observation nodes (duplicates allowed); with `weights`, one per node entry,
+        the observation terms become tau sum_i w_i e_i e_i^T (spde_set_obs_weighted)."""
         nodes = np.ascontiguousarray(nodes, dtype=np.int64)
-        key = nodes.tobytes()
-        if self._obs == key:
-            return
-        nat.check(nat.lib().spde_set_obs(self._h, nodes.ctypes.data, int(nodes.size)), self._h, "set_obs")
+        if weights is None:
+            key = nodes.tobytes()
+            if self._obs == key:
+                return
+            nat.check(nat.lib().spde_set_obs(self._h, nodes.ctypes.data, int(nodes.size)), self._h, "set_obs")
+        else:
+            w = np.ascontiguousarray(np.broadcast_to(np.asarray(weights, dtype=np.float64), nodes.shape))
+            key = nodes.tobytes() + b"w" + w.tobytes()
+            if self._obs == key:
+                return
+            nat.check(nat.lib().spde_set_obs_weighted(self._h, nodes.ctypes.data, w.ctypes.data, int(nodes.size)),
+                      self._h, "set_obs_weighted")
         self._obs = key
 
     def assemble(self, canon):

@@ -19,18 +19,30 @@ the CUDA path.  Cases:
 * ``facade_wm``  ``Model.update`` conditional mean (reference ``model.py:120-127``).
 * ``separable_*`` separable space-time models Q = Qt (x) Qs, as the ``model_*``
   cases (reference ``spdes/seperable_spatial_temporal2D.py`` and
-  ``seperable_spatial_temporal_idiffusion2D.py``).  They pin the oracle only; the
-  CUDA path does not cover this family yet, so they carry their own prefix.
+  ``seperable_spatial_temporal_idiffusion2D.py``).  They pin the oracle and,
+  through ``tests/test_gpu_separable.py``, the CUDA path's 75-slot plans; they
+  carry their own prefix because their parameter layout differs.
 
 * ``facade_cov``  ``Model.setModel(useCov=True)`` and two ``update`` calls, with
   covariate + intercept and with intercept only (reference ``model.py:120-150``).
+* ``facade_tau``  ``Model.update`` twice with different ``tau`` (the reference
+  accumulates Q += tau_k S_k^T S_k, ``model.py:120-127``), without and with fixed
+  effects.
+* ``grid_adv``  face velocities on extended grids: ``assimilate_adv`` (with the
+  ``advBound`` ramp into the padding cells) and ``evalAdv`` of the B-spline
+  velocity, plus the bases on the extended grid
+  (``grids/spat2Dtemp_regular_mesh.py:102-117,157-391``).
+* ``model_*_ext2``  model objects on a grid extended by two cells
+  (``extend=2``): the velocity field and the observations go through the
+  padding (``n2e``).
 * ``grid_getS``  the observation matrix with fixed-effect columns: ``Grid.getS``
   after ``addInt`` / ``addCov`` (with and without intercept and scaling) on a
   padded space-time grid (reference ``grids/spat2Dtemp_regular_mesh.py:35-68``).
 
 ``python tests/golden/make_golden.py --only separable [name ...]`` regenerates just
 the separable cases, ``--only getS`` the grid_getS fixture, ``--only facade_cov`` the
-facade_cov fixture.
+facade_cov fixture, ``--only facade_tau`` the facade_tau fixture, ``--only plumbing``
+the grid_adv and extended-grid model fixtures.
 """
 from __future__ import annotations
 
@@ -306,6 +318,89 @@ def facade_cov_case(sp=None):
     print("facade_cov:", {k: out[k].shape for k in out if k.endswith("_mu2")})
 
 
+def facade_tau_case(sp=None):
+    """Model.update twice with different noise precisions: plain, and with the
+    covariate + intercept fixed effects (reference model.py:120-150)."""
+    sp = sp or ref_harness.load_reference()
+    M, N = 16, 14
+    par = np.array([-0.6, 0.1, 0.2, 0.4, 2.0])
+    rng = np.random.default_rng(81)
+    cov = 1.0 + rng.uniform(0.0, 2.0, size=M * N)
+    idx1 = np.sort(rng.choice(M * N, 30, replace=False))
+    idx2 = np.sort(rng.choice(M * N, 25, replace=False))
+    y1 = rng.normal(size=30) + 2.0
+    y2 = rng.normal(size=25) + 2.0
+    tau1, tau2 = 20.0, 3.5
+    out = dict(M=M, N=N, par=par, cov=cov, idx1=idx1, idx2=idx2, y1=y1, y2=y2, tau1=tau1, tau2=tau2)
+    for name in ("plain", "cov"):
+        g = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float))
+        model = sp.Model(spde="whittle-matern", grid=g, parameters=par, ani=True, ha=False, bc=3)
+        if name == "cov":
+            model.setModel(mu=cov, sigmas=np.log(np.array([0.01, 140.0])), useCov=True, scale=True)
+        else:
+            model.setModel()
+        model.update(y1, idx1, tau=tau1)
+        out[f"{name}_mu1"] = model.mu.copy()
+        model.update(y2, idx2, tau=tau2)
+        out[f"{name}_mu2"] = model.mu.copy()
+        if name == "plain":
+            out.update({f"plain_{k}": v for k, v in _csr(model.Q).items()})
+    np.savez_compressed(os.path.join(OUT, "facade_tau.npz"), **out)
+    print("facade_tau:", {k: float(np.linalg.norm(out[k])) for k in out if k.endswith("_mu2")})
+
+
+def plumbing_cases(sp=None):
+    """Face velocities and bases on extended grids, and two model objects on a
+    grid extended by two cells (reference grids/spat2Dtemp_regular_mesh.py:
+    102-117 extend, 157-275 bases, 277-391 assimilate_adv / advBound)."""
+    sp = sp or ref_harness.load_reference()
+    M, N, T = 9, 7, 3
+    rng = np.random.default_rng(91)
+    we = rng.normal(size=M * N)
+    wn = rng.normal(size=M * N)
+    par_adv = 0.3 * rng.normal(size=18)
+    out = dict(M=M, N=N, T=T, we=we, wn=wn, par_adv=par_adv)
+    for ext in (0, 1, 2, 3):
+        g = sp.grid(x=np.arange(M, dtype=float), y=np.arange(N, dtype=float), t=np.arange(T, dtype=float),
+                    extend=ext if ext else None)
+        out[f"ww_e{ext}"] = g.assimilate_adv(we, wn)
+        out[f"adv_e{ext}"] = g.evalAdv(par_adv)
+        out[f"bs_e{ext}"] = g.bs
+        out[f"bsH_e{ext}"] = g.bsH
+    np.savez_compressed(os.path.join(OUT, "grid_adv.npz"), **out)
+    print("grid_adv:", {k: out[k].shape for k in out if k.startswith("ww_")})
+
+    from spdepy.spdes.cov_advection_var_diffusion2D import CovAdvectionVarDiffusion2D
+    M, N, T = 9, 8, 4
+    g, gi = _st_grid(sp, M, N, T, extend=2)
+    rng = np.random.default_rng(92)
+    ww = _smooth_ww(g, seed=93)
+    par = np.hstack([np.log(0.4) + 0.1 * rng.normal(size=9), np.log(0.6) + 0.1 * rng.normal(size=9),
+                     0.3 * rng.normal(size=9), 0.3 * rng.normal(size=9), 0.8, 0.1,
+                     np.log(0.4), np.log(0.6), 0.3, 0.0, np.log(100.0)])
+    mod0 = sp.spde_init(model="whittle-matern", grid=sp.grid(x=np.arange(M, dtype=float),
+                        y=np.arange(N, dtype=float), extend=2), ani=True, ha=False, bc=3)
+    mod = CovAdvectionVarDiffusion2D(grid=g, mod0=mod0, par=par, bc=3, ww=ww)
+    mod.setQ(par)
+    idx = np.random.default_rng(94).choice(M * N * T, 100, replace=False)
+    _model_case("covadv_vardiff_bc3_ext2", mod, par, idx, 0.1,
+                dict(gi, bc=3, family="cov-advection-var-diffusion", ani=1, ha=0), extra=dict(ww=ww))
+
+    M, N, T = 8, 8, 4
+    g, gi = _st_grid(sp, M, N, T, extend=2)
+    rng = np.random.default_rng(95)
+    par = np.hstack([np.log(0.4) + 0.1 * rng.normal(size=9), np.log(0.6) + 0.1 * rng.normal(size=9),
+                     0.3 * rng.normal(size=9), 0.3 * rng.normal(size=9), 0.2 * rng.normal(size=9),
+                     0.2 * rng.normal(size=9), 0.1, np.log(0.4), np.log(0.6), 0.3, 0.0, np.log(100.0)])
+    mod0 = sp.spde_init(model="whittle-matern", grid=sp.grid(x=np.arange(M, dtype=float),
+                        y=np.arange(N, dtype=float), extend=2), ani=True, ha=False, bc=3)
+    mod = sp.spde_init(model="var-advection-var-diffusion", grid=g, parameters=par, ani=True, ha=False, bc=3,
+                       mod0=mod0)
+    idx = np.random.default_rng(96).choice(M * N * T, 90, replace=False)
+    _model_case("varadv_vardiff_bc3_ext2", mod, par, idx, 0.1,
+                dict(gi, bc=3, family="var-advection-var-diffusion", ani=1, ha=0))
+
+
 def getS_cases(sp=None):
     """Grid.getS with fixed-effect columns on a padded space-time grid."""
     sp = sp or ref_harness.load_reference()
@@ -388,8 +483,14 @@ if __name__ == "__main__":
         getS_cases()
     elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "facade_cov":
         facade_cov_case()
+    elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "facade_tau":
+        facade_tau_case()
+    elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "plumbing":
+        plumbing_cases()
     else:
         main()
         separable_cases()
         getS_cases()
         facade_cov_case()
+        facade_tau_case()
+        plumbing_cases()

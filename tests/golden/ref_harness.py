@@ -30,7 +30,9 @@ import types
 
 import numpy as np
 
-REF_SRC = "/root/reference/src/spdepy"
+# the reference project root: $SPDEPY_REFERENCE, by default where this container mounts it
+REF_ROOT = os.environ.get("SPDEPY_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src", "spdepy")
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 REF_LIBS = os.path.join(REPO, "oracle", "_ref")

@@ -12,7 +12,7 @@ def model_cases():
 
 
 def separable_cases():
-    """Separable space-time fixtures (oracle only: the CUDA path does not cover the family yet)."""
+    """Separable space-time fixtures (the oracle and the CUDA path's 75-slot plans)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "separable_*.npz")))
 
 

@@ -1,0 +1,97 @@
+"""Failure detection on the GPU path, made on the host side (no kernel is made to
+fault): invalid parameters, a matrix that is not positive definite, a PCG that
+runs out of iterations.  Each must come back as the C ABI's status code and the
+Python error the reference raises in the same place (CHOLMOD's
+CholmodNotPositiveDefiniteError for a non-SPD factorisation), and leave the
+plan usable for the next call."""
+import numpy as np
+import pytest
+
+from golden_cases import load
+from gpu_cases import gpu_model
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from spdepy_gb300 import build
+    build.build()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nan_parameter_is_an_argument_error(precision):
+    from spdepy_gb300 import _native as nat
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, precision)
+    par = np.array(g["par"], float)
+    bad = par.copy()
+    bad[1] = np.nan
+    with pytest.raises(nat.SpdeError, match="invalid argument.*non-finite"):
+        mod.logLike(bad, grad=True)
+    canon = mod.canonical(bad)
+    assert nat.lib().spde_assemble(mod.plan.h, canon.ctypes.data, canon.size) == 1
+    f = mod.logLike(par, grad=False)  # the plan still works
+    assert abs(f - float(g["f"])) <= 1e-6 * abs(float(g["f"]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_indefinite_matrix_raises_not_positive_definite(precision):
+    """Q + tau S^T S with a large negative tau has negative diagonal entries: the
+    factorisation reports SPDE_ERR_NOT_SPD, which the Python layer raises as
+    NotPositiveDefiniteError, and the next factorisation succeeds."""
+    import ctypes
+    from spdepy_gb300 import _native as nat
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, precision)
+    mod._assemble(g["par"])
+    plan = mod.plan
+    plan.set_obs(mod.grid.obs_nodes(g["idx"]))
+    ld = ctypes.c_double()
+    assert nat.lib().spde_factor(plan.h, 1, -1e6, ctypes.byref(ld)) == 3
+    assert b"not positive definite" in nat.lib().spde_last_error(plan.h)
+    with pytest.raises(nat.NotPositiveDefiniteError):
+        plan.factor(True, -1e6)
+    ld_ok = plan.factor(True, 400.0)
+    assert np.isfinite(ld_ok)
+
+
+def test_pcg_iteration_cap_reports_not_converged():
+    """PCG that reaches maxit before the tolerance returns SPDE_ERR_NOT_CONVERGED
+    with the iterations run and the residual reached."""
+    import ctypes
+    from spdepy_gb300 import _native as nat
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, "fp64")
+    mod._assemble(g["par"])
+    plan = mod.plan
+    n = mod.grid.n
+    b = torch.randn(n, dtype=torch.float64, generator=torch.Generator().manual_seed(0)).cuda()
+    x = torch.empty_like(b)
+    it, rel = ctypes.c_int(), ctypes.c_double()
+    rc = nat.lib().spde_pcg(plan.h, 0, 0.0, 1, None, b.data_ptr(), x.data_ptr(), 1, 1e-12, 3, ctypes.byref(it),
+                            ctypes.byref(rel))
+    assert rc == 6
+    assert it.value == 3 and rel.value > 1e-12
+    with pytest.raises(nat.SpdeError, match="not converged"):
+        plan.pcg(b, precond="jacobi", tol=1e-12, maxit=3, check=True)
+    x2, its, rel2 = plan.pcg(b, precond="jacobi", tol=1e-8, maxit=5000)
+    assert rel2 <= 1e-8
+
+
+def test_bad_observation_index_and_weights():
+    from spdepy_gb300 import _native as nat
+    g = load("advdiff_ani_bc3")
+    mod = gpu_model(g, "fp64")
+    plan = mod.plan
+    n = mod.grid.n
+    with pytest.raises(nat.SpdeError, match="out of range"):
+        plan.set_obs(np.array([0, n], dtype=np.int64))
+    plan._obs = None
+    with pytest.raises(nat.SpdeError, match="finite and non-negative"):
+        plan.set_obs(np.array([0, 1], dtype=np.int64), weights=np.array([1.0, -2.0]))
+    plan._obs = None
+    plan.set_obs(np.array([0, 1], dtype=np.int64), weights=np.array([1.0, 2.0]))

@@ -207,3 +207,91 @@ def test_separable_host_mapping(name):
         ok = (x + dx >= 0) & (x + dx < Mx) & (y + dy >= 0) & (y + dy < Ny) & (t + dt >= 0) & (t + dt < T)
         qv[ok, s] = np.asarray(Q[k[ok], (((t + dt) * Ny + y + dy) * Mx + x + dx)[ok]]).ravel()
     assert abs(stencil_to_csr(grid, qv) - Q).max() == 0.0
+
+
+@pytest.mark.parametrize("ext", [0, 1, 2, 3])
+def test_grid_plumbing_on_extended_grids(ext):
+    """Face velocities and bases on grids padded by `ext` cells against the
+    reference's own output: assimilate_adv with the advBound ramp into the
+    padding, evalAdv of a B-spline velocity (through the extended bsA), and the
+    centre / face bases (grids/spat2Dtemp_regular_mesh.py:102-117,157-391)."""
+    from oracle.spde_oracle import OracleGrid
+    from spdepy_gb300.grids import Grid
+    g = load("grid_adv.npz")
+    M, N, T = (int(g[k]) for k in ("M", "N", "T"))
+    args = (np.arange(M, dtype=float), np.arange(N, dtype=float), np.arange(T, dtype=float), ext or None)
+    p = g["par_adv"]
+    nb = p.size // 2
+    for grid in (Grid(*args), OracleGrid(*args)):
+        ww = grid.assimilate_adv(g["we"], g["wn"])
+        assert np.allclose(ww, g[f"ww_e{ext}"], rtol=1e-14, atol=1e-15), type(grid)
+        assert np.allclose(grid.bs, g[f"bs_e{ext}"], rtol=1e-12, atol=1e-14), type(grid)
+        assert np.allclose(grid.bsH, g[f"bsH_e{ext}"], rtol=1e-12, atol=1e-14), type(grid)
+    grid = Grid(*args)
+    A = grid.bsA
+    adv = np.stack([A[:, 0] @ p[:nb], A[:, 1] @ p[nb:], A[:, 2] @ p[:nb], A[:, 3] @ p[nb:]], axis=1)
+    assert np.allclose(adv, g[f"adv_e{ext}"], rtol=1e-12, atol=1e-14)
+    assert np.allclose(OracleGrid(*args).evalAdv(p), g[f"adv_e{ext}"], rtol=1e-12, atol=1e-14)
+
+
+def test_updates_with_different_tau():
+    """Two Model.update calls with different noise precisions accumulate
+    Q += tau_k S_k^T S_k (reference model.py:120-127): the conditional means of
+    the reference, without fixed effects (dense solves of the accumulated
+    precision) and with them (block elimination through the border)."""
+    from oracle.spde_oracle import OracleGrid, OracleModel
+    from spdepy_gb300.fixed_effects import Border, update_step
+    g = load("facade_tau.npz")
+    M, N = int(g["M"]), int(g["N"])
+    Q = OracleModel(OracleGrid(np.arange(M, dtype=float), np.arange(N, dtype=float)), "whittle-matern", "ani",
+                    3).makeQ(g["par"]).toarray()
+    taus = (float(g["tau1"]), float(g["tau2"]))
+    A = Q.copy()
+    mu = np.zeros(M * N)
+    for k, tau in zip((1, 2), taus):
+        idx, y = g[f"idx{k}"], g[f"y{k}"]
+        np.add.at(A, (idx, idx), tau)
+        b = np.zeros(M * N)
+        np.add.at(b, idx, tau * (y - mu[idx]))
+        mu = mu + np.linalg.solve(A, b)
+        assert np.allclose(mu, g[f"plain_mu{k}"], rtol=1e-10, atol=1e-12 * np.abs(mu).max()), k
+    Qref = sparse.csr_matrix((g["plain_Q_data"], g["plain_Q_indices"], g["plain_Q_indptr"]), shape=A.shape)
+    assert abs(Qref - sparse.csr_matrix(A)).max() <= 1e-12 * abs(Qref).max()
+    grid, mu = _fixed_effect_setup(dict(M=M, N=N, cov=g["cov"]), "cov")
+    border = Border(grid.n, np.exp(np.log(np.array([0.01, 140.0]))))
+    A = Q.copy()
+    F = grid._fixed_effects()
+    for k, tau in zip((1, 2), taus):
+        idx, y = g[f"idx{k}"], g[f"y{k}"]
+        nodes = grid.obs_nodes(idx)
+        np.add.at(A, (nodes, nodes), tau)
+        mu = update_step(border, lambda R: np.linalg.solve(A, R), mu, nodes, F[idx], y, tau)
+        ref = g[f"cov_mu{k}"]
+        assert np.allclose(mu, ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max()), k
+
+
+def test_fixed_effect_marginal_variances_formula():
+    """The reference's qinv with fixed effects returns diag((S Q_aug S^T)^-1) for
+    S = getS() = [I | X] (model.py:108-117); the facade computes it as the
+    selected inverse of the lattice block A plus a Woodbury correction for the
+    border.  Here both sides are dense on a small case."""
+    from spdepy_gb300.fixed_effects import Border
+    rng = np.random.default_rng(9)
+    n, p = 40, 2
+    R = rng.normal(size=(n, n))
+    A0 = R @ R.T + n * np.eye(n)
+    X = np.column_stack([np.ones(n), rng.uniform(0.5, 2.0, n)])
+    border = Border(n, [0.3, 4.0])
+    nodes = rng.choice(n, 15, replace=False)
+    border.add(nodes, X[nodes], 7.0)
+    A = A0.copy()
+    np.add.at(A, (nodes, nodes), 7.0)
+    Qaug = np.block([[A, border.B], [border.B.T, border.C]])
+    S = np.hstack([np.eye(n), X])
+    ref = np.diag(np.linalg.inv(S @ Qaug @ S.T))
+    U = np.hstack([X, border.B])
+    Y = np.linalg.solve(A, U)
+    Winv = np.block([[np.zeros((p, p)), np.eye(p)], [np.eye(p), -border.C]])
+    K = np.linalg.inv(Winv + U.T @ Y)
+    got = np.diag(np.linalg.inv(A)) - np.einsum("ij,ij->i", Y @ K, Y)
+    assert np.allclose(got, ref, rtol=1e-10, atol=0)
