@@ -131,6 +131,13 @@ int spde_plan_read_sites(SpdePlan* plan, double* ms, double* flops, int64_t* til
  * the two factorisations' latency-bound top levels overlap; it doubles the
  * factor and inverse memory.  1 runs them one after the other on one set. */
 int spde_plan_set_pipelines(SpdePlan* plan, int pipelines);
+/* Failure detection (no reference counterpart): every wait inside the
+ * tensor-core kernels gives up after this many nanoseconds of wall clock (0
+ * restores the default, 2 s); the kernel then records an error, waits for its
+ * issued tensor-core work, frees its tensor memory and returns, and the
+ * factorisation or inversion returns SPDE_ERR_CUDA with the plan still usable.
+ * Tests lower the limit to make the waits run out. */
+int spde_plan_set_wait_limit(SpdePlan* plan, int64_t ns);
 /* Symbolic analysis without a GPU (host only): statistics and the ordering. */
 int spde_symbolic_info(int Mx, int Ny, int T, int leaf_max, SpdePlanInfo* info);
 int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int32_t* front_ns, int32_t* front_nb,

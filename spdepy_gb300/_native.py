@@ -60,6 +60,7 @@ SIGNATURES = {
     "spde_plan_read_profile": (_I, [_P, _P, _P, _P, _I]),
     "spde_plan_read_sites": (_I, [_P, _P, _P, _P, _I]),
     "spde_plan_set_pipelines": (_I, [_P, _I]),
+    "spde_plan_set_wait_limit": (_I, [_P, _I64]),
     "spde_symbolic_info": (_I, [_I, _I, _I, _I, ctypes.POINTER(PlanInfo)]),
     "spde_symbolic_export": (_I, [_I, _I, _I, _I, _P, _P, _P, _P, _I64]),
     "spde_set_model": (_I, [_P, ctypes.POINTER(ModelDesc)]),

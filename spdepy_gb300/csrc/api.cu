@@ -327,6 +327,7 @@ static void share_model(const Plan& p, Plan& t) {
   t.nobs = p.nobs;
   t.profile = p.profile;
   t.profile_tc_only = p.profile_tc_only;
+  t.tc_wait_ns = p.tc_wait_ns;
 }
 
 // The learned preconditioner reads the 43-slot spatio-temporal stencil and the
@@ -843,6 +844,14 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   const double trace_term = exact ? tr : tr / nh1;
   g[ntheta - 1] = m * r / 2.0 - 0.5 * r * tau * trace_term - tau / 2 * rss;
   for (int i = 0; i < ntheta; ++i) jac[i] = -g[i] / (double(m) * r);
+  return SPDE_OK;
+}
+
+int spde_plan_set_wait_limit(SpdePlan* plan, int64_t ns) {
+  if (!plan || ns < 0) return SPDE_ERR_ARG;
+  const unsigned long long v = ns == 0 ? kTcWaitNs : static_cast<unsigned long long>(ns);
+  plan->p.tc_wait_ns = v;
+  if (plan->twin) plan->twin->tc_wait_ns = v;
   return SPDE_OK;
 }
 

@@ -380,7 +380,7 @@ bool tc_gemm_enabled() {
 
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout, int blayout,
-                 cudaStream_t st, int path, int nmax) {
+                 cudaStream_t st, int path, int nmax, unsigned long long wait_ns) {
   if (ntasks <= 0) return;
   if (path == kPathNarrow) {
     switch (mode) {
@@ -406,7 +406,7 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
     }
     if (path == kPathTensor && tc_gemm_enabled()) {
       launch_gemm_tc(tasks, ntasks, reinterpret_cast<const float*>(A), reinterpret_cast<const float*>(B),
-                     reinterpret_cast<float*>(C), mode, alayout, blayout, st);
+                     reinterpret_cast<float*>(C), mode, alayout, blayout, st, wait_ns);
       return;
     }
   }
@@ -419,9 +419,9 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
 }
 
 template void launch_gemm<double>(const GemmTask*, int, const double*, const double*, double*, int, int, int,
-                                  cudaStream_t, int, int);
+                                  cudaStream_t, int, int, unsigned long long);
 template void launch_gemm<float>(const GemmTask*, int, const float*, const float*, float*, int, int, int,
-                                 cudaStream_t, int, int);
+                                 cudaStream_t, int, int, unsigned long long);
 
 // --------------------------------------------------- diagonal block POTRF
 // Cholesky factor and inverse of one w x w diagonal block (w <= 64) per CTA.

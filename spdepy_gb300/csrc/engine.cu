@@ -16,6 +16,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <cudaTypedefs.h>
+
 #include "engine.cuh"
 
 namespace spde {
@@ -53,16 +55,39 @@ void Schedule::upload() {
   d_mirror = upload_vec(mirror);
 }
 void Schedule::release() {
-  cudaFree(d_gemm); cudaFree(d_diag); cudaFree(d_ext); cudaFree(d_rows); cudaFree(d_mirror);
-  d_gemm = nullptr; d_diag = nullptr; d_ext = nullptr; d_rows = nullptr; d_mirror = nullptr;
+  cudaFree(d_gemm); cudaFree(d_diag); cudaFree(d_ext); cudaFree(d_rows); cudaFree(d_mirror); cudaFree(d_maps);
+  d_gemm = nullptr; d_diag = nullptr; d_ext = nullptr; d_rows = nullptr; d_mirror = nullptr; d_maps = nullptr;
 }
 
 // ----------------------------------------------------------- schedule helpers
 struct Builder {
   Schedule& s;
   int TM, TN;
+  bool pair_ok;   // products of at least 128 x 128 x 128 may take 256 x 256 cluster-pair tiles (FP32 plan)
   int depth = 0;  // tree depth of the ops begun next
-  explicit Builder(Schedule& sc, int tm, int tn) : s(sc), TM(tm), TN(tn) {}
+  explicit Builder(Schedule& sc, int tm, int tn, bool pairs = false) : s(sc), TM(tm), TN(tn), pair_ok(pairs) {}
+
+  // TMA source of a row-major operand starting at element `off` of buffer `buf`,
+  // inside the region [base, ...) with row stride ld: the map index and the
+  // (column, row) coordinates, or -1 where TMA cannot address it (alignment)
+  int tma_source(int buf, int64_t base, int64_t off, int ld, int* x, int* y) {
+    if (buf == B_NONE || base < 0 || (ld & 3) != 0 || (base & 3) != 0 || off < base) return -1;
+    const int64_t d = off - base, col = d % ld, row = d / ld;
+    if ((col & 3) != 0 || row > int64_t(1) << 30) return -1;
+    const auto key = std::make_tuple(buf, base, ld);
+    auto it = s.map_index.find(key);
+    int idx;
+    if (it == s.map_index.end()) {
+      idx = int(s.maps.size());
+      s.maps.push_back({buf, base, ld});
+      s.map_index.emplace(key, idx);
+    } else {
+      idx = it->second;
+    }
+    *x = int(col);
+    *y = int(row);
+    return idx;
+  }
 
   Op& begin(int kind) {
     s.ops.push_back(Op());
@@ -86,6 +111,27 @@ struct Builder {
   // the others on the tensor-core kernel: split one GEMM launch into two, the
   // first (already complete) and the second left for finish().
   void split_by_k() {
+    {
+      // cluster-pair tasks go first, in a launch of their own
+      Op& o = s.ops.back();
+      const int64_t beg = o.off, end = int64_t(s.gemm.size());
+      auto mid = std::stable_partition(s.gemm.begin() + beg, s.gemm.begin() + end,
+                                       [](const GemmTask& t) { return t.pair != 0; });
+      const int64_t npair = int64_t(mid - s.gemm.begin()) - beg;
+      if (npair > 0) {
+        o.tc = kPathPair;
+        if (beg + npair == end) return;
+        Op rest = o;
+        o.flops = 0;
+        for (int64_t i = beg; i < beg + npair; ++i) o.flops += 2.0 * s.gemm[i].m * s.gemm[i].n * s.gemm[i].k;
+        o.count = int(npair);
+        ++s.launches;
+        rest.off = beg + npair;
+        rest.flops = 0;
+        for (int64_t i = beg + npair; i < end; ++i) rest.flops += 2.0 * s.gemm[i].m * s.gemm[i].n * s.gemm[i].k;
+        s.ops.push_back(rest);
+      }
+    }
     Op& o = s.ops.back();
     const int64_t beg = o.off, end = int64_t(s.gemm.size());
     int nmax = 0;
@@ -139,14 +185,22 @@ struct Builder {
   // kt: skip structurally zero K ranges of triangular row-layout operands whose
   // K index shares the origin of their row index (KT_A_UPPER: A[i,k] = 0 for
   // k < i; KT_B_LOWER: B[j,k] = 0 for k > j; KT_BOTH_UPPER: both upper).
+  // abase / bbase: start of the row-major region the operand lies in (for its
+  // TMA map); with both given, a product of at least 128 x 128 x 128 in the FP32
+  // plan takes 256 x 256 tiles for the cluster-pair tensor-core kernel.
   void gemm_tiles(int64_t a, int lda, int64_t arow, int64_t b, int ldb, int64_t brow, int64_t c, int ldc, int m, int n,
-                  int k, bool lower = false, int i_start = 0, int kt = KT_NONE) {
+                  int k, bool lower = false, int i_start = 0, int kt = KT_NONE, int64_t abase = -1,
+                  int64_t bbase = -1) {
     if (m <= 0 || n <= 0 || k <= 0) return;
-    for (int j0 = 0; j0 < n; j0 += TN)
-      for (int i0 = lower ? std::max(j0, i_start) : i_start; i0 < m; i0 += TM) {
+    const Op& op = s.ops.back();
+    const bool pair = pair_ok && abase >= 0 && bbase >= 0 && arow == lda && brow == ldb && op.al == kRow &&
+                      op.bl == kRow && m >= 128 && n >= 128 && k >= 128 && i_start == 0;
+    const int tm = pair ? kPairTile : TM, tn = pair ? kPairTile : TN;
+    for (int j0 = 0; j0 < n; j0 += tn)
+      for (int i0 = lower ? std::max(j0, i_start) : i_start; i0 < m; i0 += tm) {
         int klo = 0, khi = k;
         if (kt == KT_A_UPPER) klo = std::min(i0, k);
-        else if (kt == KT_B_LOWER) khi = std::min(k, j0 + TN);
+        else if (kt == KT_B_LOWER) khi = std::min(k, j0 + tn);
         else if (kt == KT_BOTH_UPPER) klo = std::min(std::max(i0, j0), k);
         if (khi <= klo) { klo = 0; khi = std::min(k, 1); }
         GemmTask t;
@@ -154,9 +208,14 @@ struct Builder {
         t.b = b + int64_t(j0) * brow + klo;
         t.c = c + int64_t(i0) * ldc + j0;
         t.lda = lda; t.ldb = ldb; t.ldc = ldc;
-        t.m = std::min(TM, m - i0);
-        t.n = std::min(TN, n - j0);
+        t.m = std::min(tm, m - i0);
+        t.n = std::min(tn, n - j0);
         t.k = khi - klo;
+        if (pair) {
+          t.pair = 1;
+          t.amap = tma_source(op.abuf, abase, t.a, lda, &t.ax, &t.ay);
+          t.bmap = tma_source(op.bbuf, bbase, t.b, ldb, &t.bx, &t.by);
+        }
         s.gemm.push_back(t);
         s.ops.back().flops += 2.0 * t.m * t.n * t.k;
       }
@@ -181,8 +240,8 @@ struct Builder {
 
 static inline int nblocks(int ns) { return (ns + kNbk - 1) / kNbk; }
 
-static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int TN) {
-  Builder b(sc, TM, TN);
+static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, bool pairs) {
+  Builder b(sc, TM, TN, pairs);
   const auto& F = S.fronts;
   for (int d = S.max_depth; d >= 0; --d) {
     const auto& fr = S.by_depth[d];
@@ -260,7 +319,7 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         int rows = x.ns + x.nb - c0, cols = c1 - c0;
         int64_t a = x.p_off + int64_t(c0) * x.ld + k0;
         b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.p_off + int64_t(c0) * x.ld + c0, x.ld, rows, cols,
-                     kb * kNbk + w - k0, true);
+                     kb * kNbk + w - k0, true, 0, KT_NONE, x.p_off, x.p_off);
       }
       b.end();
       // at the end of a panel: one update of all later separator columns with K = panel width
@@ -274,7 +333,7 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
           int rows = x.ns + x.nb - pend, cols = x.ns - pend;
           int64_t a = x.p_off + int64_t(pend) * x.ld + pstart;
           b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.p_off + int64_t(pend) * x.ld + pend, x.ld, rows, cols,
-                       kPanel, true);
+                       kPanel, true, 0, KT_NONE, x.p_off, x.p_off);
         }
         b.end();
       }
@@ -287,7 +346,7 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       const Front& x = F[f];
       if (x.nb == 0) continue;
       int64_t a = x.p_off + int64_t(x.ns) * x.ld;
-      b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.u_off, x.ldu, x.nb, x.nb, x.ns, true);
+      b.gemm_tiles(a, x.ld, x.ld, a, x.ld, x.ld, x.u_off, x.ldu, x.nb, x.nb, x.ns, true, 0, KT_NONE, x.p_off, x.p_off);
     }
     b.end();
   }
@@ -415,8 +474,9 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
 // reads its operands row by row (K contiguous).  W and W^T are both kept
 // (row-major); for a node [a, b) of the halving tree with children [a, m), [m, b):
 //   TT = W_11^T L_21^T,  (W^T)_12 = -TT W_22^T,  W_21 = ((W^T)_12)^T.
-static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, int64_t* scratch_elems) {
-  Builder b(sc, TM, TN);
+static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, int64_t* scratch_elems,
+                                  bool pairs) {
+  Builder b(sc, TM, TN, pairs);
   const auto& F = S.fronts;
   auto r4 = [](int64_t v) { return (v + 3) / 4 * 4; };
   int64_t scratch = 32;
@@ -552,7 +612,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         const Front& x = F[fr[q]];
         if (x.nb == 0) continue;
         b.gemm_tiles(sx[q].wt, sx[q].ldw, sx[q].ldw, x.p_off + int64_t(x.ns) * x.ld, x.ld, x.ld, sx[q].xt, sx[q].ldx,
-                     x.ns, x.nb, x.ns, false, 0, KT_A_UPPER);
+                     x.ns, x.nb, x.ns, false, 0, KT_A_UPPER, sx[q].wt, x.p_off);
       }
       b.end();
     }
@@ -564,7 +624,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         const Front& x = F[fr[q]];
         if (x.nb == 0) continue;
         b.gemm_tiles(sx[q].xt, sx[q].ldx, sx[q].ldx, x.z_off + int64_t(x.ns) * x.ldz + x.ns, x.ldz, x.ldz,
-                     x.z_off + x.ns, x.ldz, x.ns, x.nb, x.nb);
+                     x.z_off + x.ns, x.ldz, x.ns, x.nb, x.nb, false, 0, KT_NONE, sx[q].xt, x.z_off);
       }
       b.end();
     }
@@ -575,7 +635,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       for (size_t q = 0; q < fr.size(); ++q) {
         const Front& x = F[fr[q]];
         b.gemm_tiles(sx[q].wt, sx[q].ldw, sx[q].ldw, sx[q].wt, sx[q].ldw, sx[q].ldw, x.z_off, x.ldz, x.ns, x.ns, x.ns,
-                     true, 0, KT_BOTH_UPPER);
+                     true, 0, KT_BOTH_UPPER, sx[q].wt, sx[q].wt);
       }
       b.end();
       Op& o2 = b.begin(OP_GEMM);
@@ -585,7 +645,7 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
         const Front& x = F[fr[q]];
         if (x.nb == 0) continue;
         b.gemm_tiles(sx[q].xt, sx[q].ldx, sx[q].ldx, x.z_off + x.ns, x.ldz, x.ldz, x.z_off, x.ldz, x.ns, x.ns, x.nb,
-                     true);
+                     true, 0, KT_NONE, sx[q].xt, x.z_off);
       }
       b.end();
     }
@@ -857,7 +917,8 @@ struct Exec {
     };
     for (const Op& o : s.ops) {
       if (depth_log && (dmarks.empty() || dmarks.back().first != o.depth)) dmark(o.depth);
-      const bool on_tc = o.kind == OP_GEMM && sizeof(T) == sizeof(float) && o.tc == kPathTensor && tc_gemm_enabled();
+      const bool on_tc = o.kind == OP_GEMM && sizeof(T) == sizeof(float) &&
+                         ((o.tc == kPathTensor && tc_gemm_enabled()) || o.tc == kPathPair);
       const bool timed = p->profile && o.kind != OP_MEMSET && (on_tc || !p->profile_tc_only);
       if (timed) prof_begin(p, st);
       switch (o.kind) {
@@ -870,8 +931,16 @@ struct Exec {
           launch_potrf<T>(s.d_diag + o.off, o.count, buf(B_L), buf(B_DINV), p->d_logpiv + o.off, p->d_err, st);
           break;
         case OP_GEMM:
+          if constexpr (sizeof(T) == sizeof(float)) {
+            if (o.tc == kPathPair) {
+              launch_gemm_pair(s.d_gemm + o.off, o.count, s.d_maps, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, st,
+                               p->tc_wait_ns);
+              tc_launch_log(o);
+              break;
+            }
+          }
           launch_gemm<T>(s.d_gemm + o.off, o.count, buf(o.abuf), buf(o.bbuf), buf(o.cbuf), o.mode, o.al, o.bl, st,
-                         o.tc, o.nmax);
+                         o.tc, o.nmax, p->tc_wait_ns);
           if (on_tc) tc_launch_log(o);
           break;
         case OP_SGATHER_FWD: {
@@ -921,6 +990,61 @@ struct Exec {
   }
 };
 
+// ------------------------------------------------------------- TMA maps
+// cuTensorMapEncodeTiled, from the driver through the runtime (no libcuda link)
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return PFN_cuTensorMapEncodeTiled_v12000(nullptr);
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// Encode the schedule's TMA maps over the plan's FP32 buffers (sizes in
+// elements: factor, pool 0, pool 1, inverse scratch) and upload them.  A map
+// that cannot be encoded leaves its operands on the cp.async path.
+static void encode_maps(Plan* p, Schedule& sc, const int64_t* sizes) {
+  if (sc.maps.empty()) return;
+  const auto encode = tensor_map_encoder();
+  std::vector<CUtensorMap> host(sc.maps.size());
+  std::vector<char> ok(sc.maps.size(), 0);
+  for (size_t i = 0; i < sc.maps.size() && encode; ++i) {
+    const MapReq& r = sc.maps[i];
+    void* buf = nullptr;
+    int64_t size = 0;
+    switch (r.buf) {
+      case B_L: buf = p->d_L; size = sizes[0]; break;
+      case B_P0: buf = p->d_pool[0]; size = sizes[1]; break;
+      case B_P1: buf = p->d_pool[1]; size = sizes[2]; break;
+      case B_SX: buf = p->d_sx; size = sizes[3]; break;
+      default: break;
+    }
+    const int64_t rows = buf ? (size - r.base) / r.ld : 0;
+    if (rows < 1) continue;
+    const cuuint64_t dims[2] = {cuuint64_t(r.ld), cuuint64_t(rows)};
+    const cuuint64_t strides[1] = {cuuint64_t(r.ld) * sizeof(float)};
+    const cuuint32_t box[2] = {32, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    ok[i] = encode(&host[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, static_cast<float*>(buf) + r.base, dims, strides,
+                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  }
+  for (GemmTask& t : sc.gemm) {
+    if (t.amap >= 0 && !ok[t.amap]) t.amap = -1;
+    if (t.bmap >= 0 && !ok[t.bmap]) t.bmap = -1;
+  }
+  if (cudaMalloc(&sc.d_maps, host.size() * sizeof(CUtensorMap)) != cudaSuccess) {
+    sc.d_maps = nullptr;
+    for (GemmTask& t : sc.gemm) t.amap = t.bmap = -1;
+    return;
+  }
+  cudaMemcpy(sc.d_maps, host.data(), host.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+}
+
 // ------------------------------------------------------------------- plan API
 int plan_build(Plan* p) {
   Symbolic& S = p->sym;
@@ -954,10 +1078,16 @@ int plan_build(Plan* p) {
     p->pool_elems[k] = std::max<int64_t>(std::max(S.u_pool[k], S.z_pool[k]), 32);
     CUDA_TRY(cudaMalloc(&p->d_pool[k], size_t(p->pool_elems[k]) * es));
   }
-  build_factor_schedule(S, p->sched_factor, TM, TM);
+  const bool pairs = p->precision == 1 && tc_gemm_enabled();
+  build_factor_schedule(S, p->sched_factor, TM, TM, pairs);
   int64_t sx_elems = 0;
-  build_selinv_schedule(S, p->sched_selinv, TM, TM, &sx_elems);
+  build_selinv_schedule(S, p->sched_selinv, TM, TM, &sx_elems, pairs);
   CUDA_TRY(cudaMalloc(&p->d_sx, size_t(sx_elems) * es));
+  if (pairs) {
+    const int64_t sizes[] = {S.l_size, p->pool_elems[0], p->pool_elems[1], sx_elems};
+    encode_maps(p, p->sched_factor, sizes);
+    encode_maps(p, p->sched_selinv, sizes);
+  }
   p->sched_factor.upload();
   p->sched_selinv.upload();
   CUDA_TRY(cudaMalloc(&p->d_logpiv, std::max<size_t>(p->sched_factor.diag.size(), 1) * sizeof(double)));

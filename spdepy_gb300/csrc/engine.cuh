@@ -6,6 +6,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "assemble.cuh"
@@ -58,6 +59,15 @@ struct RowTask {
   int front, r0, r1;
 };
 
+// A TMA tensor map the cluster-pair product reads an operand through: the
+// row-major region of buffer `buf` starting at element `base`, row stride `ld`
+// (both multiples of 4), rows up to the end of the buffer.
+struct MapReq {
+  int buf;
+  int64_t base;
+  int ld;
+};
+
 struct Schedule {
   std::vector<Op> ops;
   std::vector<GemmTask> gemm;
@@ -65,12 +75,15 @@ struct Schedule {
   std::vector<ExtendTask> ext;
   std::vector<RowTask> rows;
   std::vector<MirrorTask> mirror;
+  std::vector<MapReq> maps;
+  std::map<std::tuple<int, int64_t, int>, int> map_index;
   // device copies
   GemmTask* d_gemm = nullptr;
   DiagTask* d_diag = nullptr;
   ExtendTask* d_ext = nullptr;
   RowTask* d_rows = nullptr;
   MirrorTask* d_mirror = nullptr;
+  CUtensorMap* d_maps = nullptr;
   int launches = 0;
   void upload();
   void release();
@@ -121,6 +134,8 @@ struct Plan {
   int device = 0;     // CUDA device current when the plan was created
   int precision = 1;  // 0: FP64 throughout ("plain"); 1: FP32 factor, FP64 pivots/refinement ("mixed")
   int tile_m = 64, tile_n = 64;
+  // wall-clock limit of the tensor-core kernels' pipeline waits (failure-detection tests lower it)
+  unsigned long long tc_wait_ns = kTcWaitNs;
   cudaStream_t stream = nullptr;
   // symbolic data on the device
   DevFront* d_fronts = nullptr;

@@ -1,5 +1,6 @@
 // Kernel launch interfaces shared by the CUDA translation units.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -13,6 +14,12 @@ struct GemmTask {
   int64_t a, b, c;
   int lda, ldb, ldc;
   int m, n, k;
+  // cluster-pair tasks (256 x 256 tiles, tc_gemm.cu): tensor-map index of the
+  // A / B operand (-1: loaded by cp.async) and the TMA coordinates (column,
+  // row) of the task's first element in that map
+  int amap = -1, bmap = -1;
+  int ax = 0, ay = 0, bx = 0, by = 0;
+  int pair = 0;
 };
 
 enum GemmMode { kSub = 0, kStore = 1, kNegStore = 2, kAdd = 3 };
@@ -42,19 +49,27 @@ struct DevFront {
 };
 
 // product paths: CUDA-core tiles, tensor-core tiles (FP32 only), narrow (n <= 8
-// columns), panel solve (FP32: m <= 128, n <= 64, k <= 64; CUDA-core tiles otherwise)
-enum GemmPath { kPathSimt = 0, kPathTensor = 1, kPathNarrow = 2, kPathPanel = 3 };
+// columns), panel solve (FP32: m <= 128, n <= 64, k <= 64; CUDA-core tiles
+// otherwise), 256 x 256 tiles on a cluster pair of tensor-core CTAs (FP32)
+enum GemmPath { kPathSimt = 0, kPathTensor = 1, kPathNarrow = 2, kPathPanel = 3, kPathPair = 4 };
+constexpr int kPairTile = 256;
+// default wall-clock limit of every bounded wait in the tensor-core kernels
+constexpr unsigned long long kTcWaitNs = 2000000000ull;
 constexpr int kNarrowMaxN = 8;
 
 // nmax bounds the tasks' n on the narrow path (1 selects the one-column kernel).
 template <typename T>
 void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C, int mode, int alayout,
-                 int blayout, cudaStream_t st, int path = kPathTensor, int nmax = kNarrowMaxN);
+                 int blayout, cudaStream_t st, int path = kPathTensor, int nmax = kNarrowMaxN,
+                 unsigned long long wait_ns = kTcWaitNs);
 
 // tcgen05 path for FP32 (tc_gemm.cu); tc_gemm_take_error returns and clears the
 // bounded-wait error flag of that kernel.
 void launch_gemm_tc(const GemmTask* tasks, int ntasks, const float* A, const float* B, float* C, int mode, int al,
-                    int bl, cudaStream_t st);
+                    int bl, cudaStream_t st, unsigned long long wait_ns = kTcWaitNs);
+// cluster-pair path (row-major A and B): one 2-CTA cluster per 256 x 256 task
+void launch_gemm_pair(const GemmTask* tasks, int ntasks, const CUtensorMap* maps, const float* A, const float* B,
+                      float* C, int mode, cudaStream_t st, unsigned long long wait_ns = kTcWaitNs);
 int tc_gemm_take_error(cudaStream_t st);
 bool tc_gemm_enabled();
 
