@@ -95,3 +95,39 @@ def test_bad_observation_index_and_weights():
         plan.set_obs(np.array([0, 1], dtype=np.int64), weights=np.array([1.0, -2.0]))
     plan._obs = None
     plan.set_obs(np.array([0, 1], dtype=np.int64), weights=np.array([1.0, 2.0]))
+
+
+def test_tensor_core_wait_limit_returns_an_error_and_the_plan_recovers():
+    """Every wait inside the tensor-core kernels (single-CTA and cluster-pair) is
+    bounded.  With the limit lowered to 1 ns the waits run out: each CTA records
+    the error, waits for its issued tensor-core work (with the normal limit),
+    frees its tensor memory and returns; the factorisation reports SPDE_ERR_CUDA,
+    and with the default limit restored the same plan factors to the same
+    log-determinant as before."""
+    import ctypes
+    from spdepy_gb300 import _native as nat
+    from spdepy_gb300.workloads import build_model, nonstationary_advection_diffusion
+    w = nonstationary_advection_diffusion(M=48, N=48, T=12)
+    mod = build_model(w, "mixed")
+    mod._assemble(w.par)
+    plan = mod.plan
+    L = nat.lib()
+    ld0 = plan.factor(False, 0.0)
+    prof = np.zeros(10, dtype=np.int64)
+    L.spde_plan_read_profile(plan.h, None, None, None, 1)
+    nat.check(L.spde_plan_set_profiling(plan.h, 2), plan.h)
+    nat.check(L.spde_plan_set_wait_limit(plan.h, 1), plan.h)
+    ld = ctypes.c_double()
+    try:
+        rc = L.spde_factor(plan.h, 0, 0.0, ctypes.byref(ld))
+    finally:
+        nat.check(L.spde_plan_set_wait_limit(plan.h, 0), plan.h)
+        L.spde_plan_read_profile(plan.h, None, None, prof.ctypes.data, 1)
+        L.spde_plan_set_profiling(plan.h, 0)
+    assert prof[9] > 0  # tensor-core products ran (and gave up)
+    assert rc == 2
+    assert b"timed out" in L.spde_last_error(plan.h)
+    with pytest.raises(nat.SpdeError):
+        plan.solve(torch.zeros(w.grid.n, dtype=torch.float64))  # no valid factor
+    ld1 = plan.factor(False, 0.0)
+    assert ld1 == ld0
