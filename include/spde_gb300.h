@@ -36,6 +36,7 @@ extern "C" {
 #define SPDE_PRECOND_NONE 0
 #define SPDE_PRECOND_JACOBI 1
 #define SPDE_PRECOND_LEARNED 2
+#define SPDE_PRECOND_LEARNED_COMPACT 3 /* learned, weights from spde_precond_weights_compact */
 #define SPDE_PRECOND_NPARAMS 3323
 
 typedef struct SpdePlan SpdePlan;
@@ -224,6 +225,18 @@ int spde_precond_nparams(void);
  * n x 107 FP32) keeps the activations a gradient step needs. */
 int spde_precond_weights(SpdePlan* plan, int with_obs, double tau, const float* params_dev, float* w_dev,
                          float* act_dev);
+/* The same operator G with its rows stored once per (spatial cell, time class)
+ * plus once per distinct observed node: Q's stencil coefficients do not depend
+ * on time, so a node's row of A (and the network output) depends on its time
+ * step only through the classes first / interior / last step, unless the node
+ * is observed.  The compact array (FP32, device) has
+ * spde_precond_compact_size() values: a 4-value header, then 27 (3 Mx Ny +
+ * distinct observed nodes); it stays in L2 where per-node weights (27 n) would
+ * stream from HBM on every application.  Use it with
+ * SPDE_PRECOND_LEARNED_COMPACT, the same with_obs and the same observation set
+ * (a solve checks the header and returns SPDE_ERR_STATE otherwise). */
+int spde_precond_compact_size(const SpdePlan* plan, int64_t* nfloats);
+int spde_precond_weights_compact(SpdePlan* plan, int with_obs, double tau, const float* params_dev, float* w_dev);
 /* Training loss ||z - G A G^T z||^2 / (n k) for the probe block z_dev (n x k,
  * row-major, FP64) and its gradient with respect to the parameters (grad_dev,
  * SPDE_PRECOND_NPARAMS FP32). */
@@ -244,10 +257,14 @@ int spde_qsqrt(SpdePlan* plan, int transpose, const double* x_dev, double* y_dev
  * used as training probes. */
 int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, int sweeps, double* z_dev, int nrhs);
 /* x = A^-1 b by preconditioned CG (x from 0), nrhs columns row-major, FP64
- * device; precond SPDE_PRECOND_* (w_dev: G weights for LEARNED).  Stops when
- * every column reaches ||b - A x|| <= tol ||b|| (checked every 8 iterations) or
- * after maxit iterations; *relres is the worst true relative residual.
- * Returns SPDE_ERR_NOT_CONVERGED when the tolerance was not reached. */
+ * device; precond SPDE_PRECOND_* (w_dev: G weights for LEARNED, compact weights
+ * for LEARNED_COMPACT).  The iterations run in FP32 (stencil product, vectors,
+ * preconditioner); the solution is accumulated in FP64 and the residual
+ * replaced by the true FP64 residual b - A x whenever the recursive one has
+ * fallen tenfold (and every 64 iterations).  Stops when every column's true
+ * residual reaches ||b - A x|| <= tol ||b|| or after maxit iterations; *relres
+ * is the worst true relative residual.  Returns SPDE_ERR_NOT_CONVERGED when the
+ * tolerance was not reached. */
 int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float* w_dev, const double* b_dev,
              double* x_dev, int nrhs, double tol, int maxit, int* iters, double* relres);
 

@@ -79,6 +79,8 @@ SIGNATURES = {
     "spde_conditional_mean": (_I, [_P, _D, _P, _P, _P]),
     "spde_precond_nparams": (_I, []),
     "spde_precond_weights": (_I, [_P, _I, _D, _P, _P, _P]),
+    "spde_precond_compact_size": (_I, [_P, ctypes.POINTER(_I64)]),
+    "spde_precond_weights_compact": (_I, [_P, _I, _D, _P, _P]),
     "spde_precond_grad": (_I, [_P, _I, _D, _P, _P, _P, _P, _I, ctypes.POINTER(_D), _P]),
     "spde_adam_step": (_I, [_P, _P, _P, _P, _P, _I, _D, _D, _D, _D, _I]),
     "spde_qsqrt": (_I, [_P, _I, _P, _P, _I]),

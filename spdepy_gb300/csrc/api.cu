@@ -391,7 +391,8 @@ int spde_plan_destroy(SpdePlan* plan) {
   void* ptrs[] = {p.d_fronts, p.d_perm, p.d_iperm, p.d_front_of, p.d_blist, p.d_rmap, p.d_amap, p.d_L, p.d_dinv,
                   p.d_pool[0], p.d_pool[1], p.d_logpiv, p.d_err, p.d_scalar, p.d_bs, p.d_bsH, p.d_bsA, p.d_ww,
                   p.d_theta, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.d_obs_cnt,
-                  p.d_obs_idx, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0], p.d_G[1], p.d_r, p.d_x64, p.d_b64};
+                  p.d_obs_idx, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0], p.d_G[1], p.d_r, p.d_x64, p.d_b64,
+                  p.d_obs_mask, p.d_obs_rank, p.d_obs_nodes, p.d_pc32};
   for (void* q : ptrs) cudaFree(q);
   cudaFree(p.d_part);
   cudaFree(p.d_sx);
@@ -612,13 +613,35 @@ static int set_obs(SpdePlan* plan, const int64_t* idx, const double* wts, int m)
     cnt[idx[i]] += wts ? wts[i] : 1.0;
     id[i] = int(idx[i]);
   }
+  // distinct observed nodes: bitmask, per-word rank and list (node order)
+  const int64_t nwords = (int64_t(p.sym.n) + 31) / 32;
+  std::vector<uint32_t> mask(nwords, 0u);
+  std::vector<int> rank(nwords, 0), nodes;
+  for (int64_t k = 0; k < p.sym.n; ++k)
+    if (cnt[k] > 0.0) {
+      mask[k >> 5] |= 1u << (k & 31);
+      nodes.push_back(int(k));
+    }
+  for (int64_t w = 1; w < nwords; ++w) rank[w] = rank[w - 1] + __builtin_popcount(mask[w - 1]);
+  if (nodes.empty()) nodes.push_back(0);
   cudaFree(p.d_obs_cnt); cudaFree(p.d_obs_idx);
+  cudaFree(p.d_obs_mask); cudaFree(p.d_obs_rank); cudaFree(p.d_obs_nodes);
   p.d_obs_cnt = nullptr; p.d_obs_idx = nullptr;
+  p.d_obs_mask = nullptr; p.d_obs_rank = nullptr; p.d_obs_nodes = nullptr;
+  p.nob = 0;
   API_CUDA(cudaMalloc(&p.d_obs_cnt, cnt.size() * sizeof(double)));
   API_CUDA(cudaMalloc(&p.d_obs_idx, id.size() * sizeof(int)));
   API_CUDA(cudaMemcpy(p.d_obs_cnt, cnt.data(), cnt.size() * sizeof(double), cudaMemcpyHostToDevice));
   API_CUDA(cudaMemcpy(p.d_obs_idx, id.data(), id.size() * sizeof(int), cudaMemcpyHostToDevice));
+  API_CUDA(cudaMalloc(&p.d_obs_mask, size_t(nwords) * sizeof(uint32_t)));
+  API_CUDA(cudaMalloc(&p.d_obs_rank, size_t(nwords) * sizeof(int)));
+  API_CUDA(cudaMalloc(&p.d_obs_nodes, nodes.size() * sizeof(int)));
+  API_CUDA(cudaMemcpy(p.d_obs_mask, mask.data(), size_t(nwords) * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  API_CUDA(cudaMemcpy(p.d_obs_rank, rank.data(), size_t(nwords) * sizeof(int), cudaMemcpyHostToDevice));
+  API_CUDA(cudaMemcpy(p.d_obs_nodes, nodes.data(), nodes.size() * sizeof(int), cudaMemcpyHostToDevice));
+  p.nob = mask.empty() ? 0 : rank[nwords - 1] + __builtin_popcount(mask[nwords - 1]);
   p.nobs = m;
+  ++p.obs_version;
   if (p.factored == 2) p.factored = 0;
   return SPDE_OK;
 }
@@ -874,6 +897,21 @@ int spde_precond_weights(SpdePlan* plan, int with_obs, double tau, const float* 
   return pc_weights(&p, with_obs, tau, params, w, act) ? SPDE_ERR_CUDA : SPDE_OK;
 }
 
+int spde_precond_compact_size(const SpdePlan* plan, int64_t* nfloats) {
+  if (!plan || !nfloats) return SPDE_ERR_ARG;
+  *nfloats = pc_compact_floats(&plan->p);
+  return SPDE_OK;
+}
+
+int spde_precond_weights_compact(SpdePlan* plan, int with_obs, double tau, const float* params, float* w) {
+  if (!plan || !params || !w) return SPDE_ERR_ARG;
+  Plan& p = plan->p;
+  if (int rc = not_separable(p, "the learned preconditioner")) return rc;
+  if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
+  if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
+  return pc_weights_compact(&p, with_obs, tau, params, w) ? SPDE_ERR_CUDA : SPDE_OK;
+}
+
 int spde_precond_grad(SpdePlan* plan, int with_obs, double tau, const float* params, const float* w,
                       const float* act, const double* z, int k, double* loss, float* grad) {
   if (!plan || !params || !w || !act || !z || k < 1 || !loss || !grad) return SPDE_ERR_ARG;
@@ -918,11 +956,11 @@ int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, i
 
 int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, const double* V, int nh1, int precond,
                           const float* w_q, const float* w_qc, double tol, int maxit, double* jac, int* iters) {
-  if (!plan || !y || r < 1 || !V || nh1 < 1 || !jac || maxit < 1 || precond < 0 || precond > 2 ||
-      (precond == 2 && (!w_q || !w_qc)))
+  if (!plan || !y || r < 1 || !V || nh1 < 1 || !jac || maxit < 1 || precond < 0 || precond > 3 ||
+      (precond >= 2 && (!w_q || !w_qc)))
     return SPDE_ERR_ARG;
   Plan& p = plan->p;
-  if (precond == 2)
+  if (precond >= 2)
     if (int rc = not_separable(p, "the learned preconditioner")) return rc;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   if (!p.d_obs_idx || p.nobs < 1) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
@@ -942,6 +980,10 @@ int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, co
   auto solve = [&](int with_obs, const float* w, const double* b, double* x, int nrhs) -> int {
     const int rc = pcg_solve(&p, with_obs, tau, precond, w, b, x, nrhs, tol, maxit, 8, &it, &rel);
     it_total += it;
+    if (rc == 7) {
+      p.last_error = "compact preconditioner weights do not match this solve (with or without observations, or another observation set)";
+      return SPDE_ERR_STATE;
+    }
     if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
     if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
     if (rc == 6) { p.last_error = "PCG did not reach the tolerance"; return SPDE_ERR_NOT_CONVERGED; }
@@ -984,15 +1026,19 @@ int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, co
 
 int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float* w, const double* b, double* x,
              int nrhs, double tol, int maxit, int* iters, double* relres) {
-  if (!plan || !b || !x || nrhs < 1 || maxit < 1 || !iters || !relres || precond < 0 || precond > 2 ||
-      (precond == 2 && !w))
+  if (!plan || !b || !x || nrhs < 1 || maxit < 1 || !iters || !relres || precond < 0 || precond > 3 ||
+      (precond >= 2 && !w))
     return SPDE_ERR_ARG;
   Plan& p = plan->p;
-  if (precond == 2)
+  if (precond >= 2)
     if (int rc = not_separable(p, "the learned preconditioner")) return rc;
   if (!p.assembled) { p.last_error = "no assembled model"; return SPDE_ERR_STATE; }
   if (with_obs && !p.d_obs_cnt) { p.last_error = "no observations set"; return SPDE_ERR_STATE; }
   const int rc = pcg_solve(&p, with_obs, tau, precond, w, b, x, nrhs, tol, maxit, 8, iters, relres);
+  if (rc == 7) {
+    p.last_error = "compact preconditioner weights do not match this solve (with or without observations, or another observation set)";
+    return SPDE_ERR_STATE;
+  }
   if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
   if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
   if (rc == 6) { p.last_error = "PCG did not reach the tolerance"; return SPDE_ERR_NOT_CONVERGED; }

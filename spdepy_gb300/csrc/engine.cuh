@@ -168,6 +168,15 @@ struct Plan {
   double* d_obs_cnt = nullptr;  // per natural node: summed observation weights (the count when unweighted)
   int* d_obs_idx = nullptr;   // observed natural nodes (m)
   int nobs = 0;
+  // the distinct observed nodes as a bitmask over the nodes (bit p & 31 of word
+  // p >> 5), the number of set bits before each word, and their list in node
+  // order: the learned preconditioner's compact weights give observed nodes
+  // their own rows (the observation term changes their row of A)
+  uint32_t* d_obs_mask = nullptr;
+  int* d_obs_rank = nullptr;
+  int* d_obs_nodes = nullptr;
+  int nob = 0;
+  int obs_version = 0;  // incremented by every new observation set
   // factor state
   int factored = 0;  // 0 none, 1 Q, 2 Q + tau S^T S
   double factored_tau = 0.0;
@@ -201,6 +210,8 @@ struct Plan {
   // iterative solver / preconditioner scratch (pcg.cu)
   void* d_pc = nullptr;
   size_t pc_cap = 0;
+  void* d_pc32 = nullptr;  // FP32 PCG scratch (vectors and coefficient copies)
+  size_t pc32_cap = 0;
 
   QStencil qstencil() const {
     QStencil q;
@@ -231,6 +242,10 @@ int qsqrt_apply(Plan* p, int transpose, const double* x, double* y, int nrhs);
 int jacobi_smooth(Plan* p, int with_obs, double tau, double omega, int sweeps, double* z, int nrhs);
 int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const double* b, double* x, int nrhs,
               double tol, int maxit, int check_every, int* iters, double* relres);
+// learned preconditioner, compact weights: one row of G per (spatial cell, time
+// class: first step, interior, last step) and one per distinct observed node
+int64_t pc_compact_floats(const Plan* p);
+int pc_weights_compact(Plan* p, int with_obs, double tau, const float* prm, float* w);
 
 // adjoint (adjoint.cu)
 void launch_adjoint(const Plan* p, const double* gbar, double* grad_dev, double* work, cudaStream_t st);

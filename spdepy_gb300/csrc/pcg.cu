@@ -52,19 +52,13 @@ __device__ __forceinline__ bool inside(const QStencil& q, int x, int y, int t) {
   return x >= 0 && x < q.Mx && y >= 0 && y < q.Ny && t >= 0 && t < q.T;
 }
 
-// Features, network forward and G weights, one thread per node.
-__global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const double* __restrict__ obs, double tau,
-                                                         const float* __restrict__ prm, float* __restrict__ w,
-                                                         float* __restrict__ act) {
-  __shared__ float sp[kNP];
-  for (int i = threadIdx.x; i < kNP; i += blockDim.x) sp[i] = prm[i];
-  __syncthreads();
-  const int64_t n = int64_t(q.Ns) * q.T;
-  const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const int t = int(p / q.Ns), c = int(p - int64_t(t) * q.Ns);
+// Features, network forward and the 27 G weights of the row of A at (cell c,
+// time t), whose diagonal carries the observation term `obs_term`; `act`
+// (optional) receives the activations a gradient step needs.
+__device__ __forceinline__ void pc_network(const QStencil& q, int c, int t, double obs_term, const float* sp,
+                                           float* wout, float* act) {
   const int y = c / q.Mx, x = c - y * q.Mx;
-  double diag = qval(q, c, t, 0, 0, 0) + (obs ? tau * obs[p] : 0.0);
+  double diag = qval(q, c, t, 0, 0, 0) + obs_term;
   if (!(diag > 0.0)) diag = 1.0;
   const double rd = 1.0 / diag;
   float f[kFeat];
@@ -100,17 +94,65 @@ __global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const doubl
     int dx, dy, dt;
     off27(o, &dx, &dy, &dt);
     const bool in = inside(q, x + dx, y + dy, t + dt);
-    w[int64_t(o) * n + p] = in ? ((o == 13 ? 1.f : 0.f) + a) * s : 0.f;
+    wout[o] = in ? ((o == 13 ? 1.f : 0.f) + a) * s : 0.f;
   }
   if (act) {
-    float* ap = act + p * kAct;
 #pragma unroll
-    for (int j = 0; j < kFeat; ++j) ap[j] = f[j];
+    for (int j = 0; j < kFeat; ++j) act[j] = f[j];
 #pragma unroll
-    for (int j = 0; j < kHid; ++j) ap[kFeat + j] = h1[j];
+    for (int j = 0; j < kHid; ++j) act[kFeat + j] = h1[j];
 #pragma unroll
-    for (int j = 0; j < kHid; ++j) ap[kFeat + kHid + j] = h2[j];
-    ap[kAct - 1] = s;
+    for (int j = 0; j < kHid; ++j) act[kFeat + kHid + j] = h2[j];
+    act[kAct - 1] = s;
+  }
+}
+
+// G weights of every node, offset-major (w[o n + p]), one thread per node.
+__global__ void __launch_bounds__(128) pc_forward_kernel(QStencil q, const double* __restrict__ obs, double tau,
+                                                         const float* __restrict__ prm, float* __restrict__ w,
+                                                         float* __restrict__ act) {
+  __shared__ float sp[kNP];
+  for (int i = threadIdx.x; i < kNP; i += blockDim.x) sp[i] = prm[i];
+  __syncthreads();
+  const int64_t n = int64_t(q.Ns) * q.T;
+  const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int t = int(p / q.Ns), c = int(p - int64_t(t) * q.Ns);
+  float wo[kOff];
+  pc_network(q, c, t, obs ? tau * obs[p] : 0.0, sp, wo, act ? act + p * kAct : nullptr);
+#pragma unroll
+  for (int o = 0; o < kOff; ++o) w[int64_t(o) * n + p] = wo[o];
+}
+
+// Compact weights.  A node's row of A depends on its time only through three
+// classes (first step, interior steps, last step: the stencil coefficients are
+// time-invariant) unless the node is observed, so G has one row per (class,
+// cell) and one per distinct observed node: w[(k 27 + o) Ns + c] for class k,
+// then w[27 3 Ns + o nob + j] for the j-th observed node.  One thread per row.
+__global__ void __launch_bounds__(128) pc_forward_compact_kernel(QStencil q, const double* __restrict__ obs,
+                                                                 double tau, const int* __restrict__ obs_nodes,
+                                                                 int nob, const float* __restrict__ prm,
+                                                                 float* __restrict__ w) {
+  __shared__ float sp[kNP];
+  for (int i = threadIdx.x; i < kNP; i += blockDim.x) sp[i] = prm[i];
+  __syncthreads();
+  const int64_t ncls = int64_t(3) * q.Ns;
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= ncls + nob) return;
+  float wo[kOff];
+  if (e < ncls) {
+    const int k = int(e / q.Ns), c = int(e - int64_t(k) * q.Ns);
+    const int t = k == 0 ? 0 : (k == 1 ? (q.T > 2 ? 1 : 0) : q.T - 1);
+    pc_network(q, c, t, 0.0, sp, wo, nullptr);
+#pragma unroll
+    for (int o = 0; o < kOff; ++o) w[(int64_t(k) * kOff + o) * q.Ns + c] = wo[o];
+  } else {
+    const int j = int(e - ncls);
+    const int p = obs_nodes[j];
+    const int t = p / q.Ns, c = p - t * q.Ns;
+    pc_network(q, c, t, obs ? tau * obs[p] : 0.0, sp, wo, nullptr);
+#pragma unroll
+    for (int o = 0; o < kOff; ++o) w[ncls * kOff + int64_t(o) * nob + j] = wo[o];
   }
 }
 
@@ -145,27 +187,6 @@ __global__ void pc_apply_kernel(QStencil q, const float* __restrict__ w, const T
   out[e] = TOut(acc);
 }
 
-// FP32 copy of a vector: the preconditioner reads every entry from 27 nodes,
-// so converting once here keeps FP64 -> FP32 conversions (on the narrow FP64
-// pipe of this part) out of the stencil passes.
-__global__ void pc_to_f32_kernel(const double* __restrict__ x, float* __restrict__ y, int64_t len) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i < len) y[i] = float(x[i]);
-}
-
-// Jacobi: out = x / A_pp
-__global__ void pc_jacobi_kernel(QStencil q, const double* __restrict__ obs, double tau, const double* __restrict__ x,
-                                 double* __restrict__ out, int nrhs) {
-  const int n = q.Ns * q.T;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n * nrhs) return;
-  const int p = nrhs == 1 ? e : e / nrhs;
-  const int t = p / q.Ns, c = p - t * q.Ns;
-  const double d = qval(q, c, t, 0, 0, 0) + (obs ? tau * obs[p] : 0.0);
-  out[e] = double(__fdividef(float(x[e]), float(d)));  // FP32: see pc_apply_kernel
-}
-
-// e = z - v (in place into v)
 __global__ void pc_sub_kernel(const double* __restrict__ z, double* __restrict__ v, int64_t len) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i < len) v[i] = z[i] - v[i];
@@ -328,30 +349,6 @@ __global__ void pc_dot_final_kernel(const double* __restrict__ part, int nblocks
   out[r] = acc;
 }
 
-// CG updates with per-column scalars kept on the device.
-//   x += alpha p, r -= alpha Ap with alpha = rz / pAp (0 where pAp <= 0 or done)
-__global__ void pcg_xr_kernel(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
-                              const double* __restrict__ ap, const double* __restrict__ rz,
-                              const double* __restrict__ pap, const int* __restrict__ done, int64_t n, int nrhs) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= n * nrhs) return;
-  const int c = nrhs == 1 ? 0 : int(e % nrhs);
-  if (done[c]) return;
-  const double alpha = pap[c] > 0.0 ? rz[c] / pap[c] : 0.0;
-  x[e] = fma(alpha, p[e], x[e]);
-  r[e] = fma(-alpha, ap[e], r[e]);
-}
-//   p = z + beta p with beta = rz_new / rz_old
-__global__ void pcg_p_kernel(double* __restrict__ p, const double* __restrict__ z, const double* __restrict__ rzn,
-                             const double* __restrict__ rzo, const int* __restrict__ done, int64_t n, int nrhs) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= n * nrhs) return;
-  const int c = nrhs == 1 ? 0 : int(e % nrhs);
-  if (done[c]) return;
-  const double beta = rzo[c] != 0.0 ? rzn[c] / rzo[c] : 0.0;
-  p[e] = fma(beta, p[e], z[e]);
-}
-
 // z -= omega D^-1 (A z) for one damped-Jacobi sweep (az = A z)
 __global__ void jacobi_sweep_kernel(QStencil q, const double* __restrict__ obs, double tau, double omega,
                                     const double* __restrict__ az, double* __restrict__ z, int nrhs) {
@@ -395,24 +392,6 @@ double* scratch(Plan* p, size_t elems) {
     p->pc_cap = elems;
   }
   return static_cast<double*>(p->d_pc);
-}
-
-void apply_precond(Plan* p, int kind, const float* w, const double* obs, double tau, const double* r, double* z,
-                   double* tmp, int nrhs) {
-  const QStencil q = p->qstencil();
-  const int64_t len = int64_t(p->sym.n) * nrhs;
-  if (kind == 0) {
-    cudaMemcpyAsync(z, r, size_t(len) * sizeof(double), cudaMemcpyDeviceToDevice, p->stream);
-  } else if (kind == 1) {
-    pc_jacobi_kernel<<<nblk(len), 256, 0, p->stream>>>(q, obs, tau, r, z, nrhs);
-  } else {
-    // FP32 copy of r and the FP32 intermediate G r share tmp (len doubles)
-    float* r32 = reinterpret_cast<float*>(tmp);
-    float* t32 = r32 + len;
-    pc_to_f32_kernel<<<nblk(len), 256, 0, p->stream>>>(r, r32, len);
-    pc_apply_kernel<0, float, float><<<nblk(len), 256, 0, p->stream>>>(q, w, r32, t32, nrhs);
-    pc_apply_kernel<1, float, double><<<nblk(len), 256, 0, p->stream>>>(q, w, t32, z, nrhs);
-  }
 }
 
 void col_dots(Plan* p, const double* a, const double* b, int nrhs, double* part, double* out) {
@@ -471,6 +450,389 @@ __global__ void qsqrt_kernel(int Mx, int Ny, int T, const double* __restrict__ A
     if (T > 1 && t + 1 < T) acc -= sqrt(cfac * qs[c]) * x[int64_t((t + 1) * Ns + c) * nrhs + r];
   }
   out[e] = acc;
+}
+
+// ------------------------------------------------------------ FP32 PCG
+// The iteration runs in FP32 (stencil product, vectors, preconditioner): FP64
+// is a narrow pipe on this part, and an FP64 stencil product is bound by it.
+// The solution is accumulated and the residual recomputed in FP64 whenever
+// the recursive FP32 residual has fallen by kReplaceDrop (reliable updates),
+// so the reported tolerance is always met by the true FP64 residual.
+// Inside the solver every vector is stored column by column (column r of an
+// FP32 vector at v + r n), and each kernel takes its column from blockIdx.y or
+// blockIdx.z.
+
+// FP32 copies of the stencil coefficients, slot-major (cf[s Ns + c]): slots
+// 0-24 first diagonal block (T > 1), 25-49 interior diagonal block, 50-58 the
+// block to t + 1, 59-67 the neighbours' blocks to t - 1 mirrored onto this
+// cell, 68 c Qs.
+constexpr int kCoef32 = 69;
+__global__ void coef32_kernel(QStencil q, float* __restrict__ cf) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= q.Ns) return;
+  const int cy = c / q.Mx, cx = c - cy * q.Mx;
+  const int64_t Ns = q.Ns;
+  const bool st = q.T > 1 && !q.sep;
+  for (int s = 0; s < 25; ++s) {
+    cf[s * Ns + c] = st ? float(q.Q0[int64_t(c) * 25 + s]) : 0.f;
+    cf[(25 + s) * Ns + c] = float(q.QA[int64_t(c) * 25 + s]);
+  }
+  for (int s = 0; s < 9; ++s) {
+    const int dx = s % 3 - 1, dy = s / 3 - 1;
+    const bool in = cx + dx >= 0 && cx + dx < q.Mx && cy + dy >= 0 && cy + dy < q.Ny;
+    cf[(50 + s) * Ns + c] = st ? float(q.QO[int64_t(c) * 9 + s]) : 0.f;
+    cf[(59 + s) * Ns + c] = (st && in) ? float(q.QO[int64_t(c + dy * q.Mx + dx) * 9 + (8 - s)]) : 0.f;
+  }
+  cf[68 * Ns + c] = st ? float(q.cQs[c]) : 0.f;
+}
+
+// obs32[k] = tau obs[k] in FP32 (the observation term of the diagonal)
+__global__ void obs32_kernel(const double* __restrict__ obs, double tau, float* __restrict__ o32, int64_t n) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) o32[k] = float(tau * obs[k]);
+}
+
+// row-major FP64 (n x nrhs) -> column-major FP32, and x += xc back (xc = 0)
+__global__ void to32cm_kernel(const double* __restrict__ v, float* __restrict__ o, int64_t n, int nrhs) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int64_t k = e / nrhs;
+  o[(e - k * nrhs) * n + k] = float(v[e]);
+}
+__global__ void acc64cm_kernel(double* __restrict__ x, float* __restrict__ xc, int64_t n, int nrhs) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n * nrhs) return;
+  const int64_t k = e / nrhs;
+  const int64_t f = (e - k * nrhs) * n + k;
+  x[e] += double(xc[f]);
+  xc[f] = 0.f;
+}
+
+// Fixed-order block sum of one float per thread into part[] (thread 0 writes)
+__device__ __forceinline__ double block_sum(float v, float* red) {
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) s += red[w];
+  return s;
+}
+
+// Time steps per thread of the stencil product (more threads than one per cell)
+constexpr int kTch = 8;
+
+// ap = A p in FP32 for column blockIdx.y; one thread per (cell, chunk of kTch
+// time steps), and the block's partial sum of p . ap into part[col gridDim.x + block]
+__global__ void __launch_bounds__(128) spmv32c_kernel(int Mx, int Ny, int T, int sep, float qe, float qm, float qo,
+                                                      const float* __restrict__ cf, const float* __restrict__ o32,
+                                                      const float* __restrict__ pv, float* __restrict__ apv,
+                                                      double* __restrict__ part) {
+  __shared__ float red[4];
+  const int Ns = Mx * Ny;
+  const int64_t n = int64_t(Ns) * T;
+  const int col = blockIdx.y;
+  const float* x = pv + col * n;
+  float* y = apv + col * n;
+  const int nch = (T + kTch - 1) / kTch;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  float dot = 0.f;
+  if (e < Ns * nch) {
+    const int j = e / Ns, c = e - j * Ns;
+    const int cy = c / Mx, cx = c - cy * Mx;
+    const int t0 = j * kTch, t1 = min(T, t0 + kTch);
+    float qa[25];
+    uint32_t m25 = 0, m9 = 0;
+#pragma unroll
+    for (int s = 0; s < 25; ++s) {
+      const int dx = s % 5 - 2, dy = s / 5 - 2;
+      m25 |= uint32_t(cx + dx >= 0 && cx + dx < Mx && cy + dy >= 0 && cy + dy < Ny) << s;
+      qa[s] = cf[int64_t(25 + s) * Ns + c];
+    }
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+      const int dx = s % 3 - 1, dy = s / 3 - 1;
+      m9 |= uint32_t(cx + dx >= 0 && cx + dx < Mx && cy + dy >= 0 && cy + dy < Ny) << s;
+    }
+    auto spatial = [&](const float* xt) {
+      float acc = 0.f;
+#pragma unroll
+      for (int s = 0; s < 25; ++s)
+        if (m25 >> s & 1u) acc = fmaf(qa[s], xt[(s / 5 - 2) * Mx + (s % 5 - 2)], acc);
+      return acc;
+    };
+    if (sep) {
+      // Q = Qt (x) Qs: y_t = Qt_tt u_t + Qt_off (u_(t-1) + u_(t+1)), u_t = Qs x_t
+      float up = t0 > 0 ? spatial(x + int64_t(t0 - 1) * Ns + c) : 0.f;
+      float uc = spatial(x + int64_t(t0) * Ns + c);
+      for (int t = t0; t < t1; ++t) {
+        const float un = t + 1 < T ? spatial(x + int64_t(t + 1) * Ns + c) : 0.f;
+        const int64_t k = int64_t(t) * Ns + c;
+        float acc = (t == 0 || t == T - 1 ? qe : qm) * uc + qo * (up + un);
+        if (o32) acc = fmaf(o32[k], x[k], acc);
+        y[k] = acc;
+        dot = fmaf(x[k], acc, dot);
+        up = uc;
+        uc = un;
+      }
+    } else {
+      float qf[9], qb[9];
+#pragma unroll
+      for (int s = 0; s < 9; ++s) {
+        qf[s] = cf[int64_t(50 + s) * Ns + c];
+        qb[s] = cf[int64_t(59 + s) * Ns + c];
+      }
+      const float cqs = cf[int64_t(68) * Ns + c];
+      for (int t = t0; t < t1; ++t) {
+        const int64_t k = int64_t(t) * Ns + c;
+        const float* xt = x + k;
+        float acc = 0.f;
+        if (t == 0 && T > 1) {
+#pragma unroll
+          for (int s = 0; s < 25; ++s)
+            if (m25 >> s & 1u) acc = fmaf(cf[int64_t(s) * Ns + c], xt[(s / 5 - 2) * Mx + (s % 5 - 2)], acc);
+        } else {
+          acc = spatial(xt);
+        }
+        if (T > 1) {
+          if (t < T - 1) acc = fmaf(cqs, xt[0], acc);
+          if (t + 1 < T) {
+#pragma unroll
+            for (int s = 0; s < 9; ++s)
+              if (m9 >> s & 1u) acc = fmaf(qf[s], xt[Ns + (s / 3 - 1) * Mx + (s % 3 - 1)], acc);
+          }
+          if (t > 0) {
+#pragma unroll
+            for (int s = 0; s < 9; ++s)
+              if (m9 >> s & 1u) acc = fmaf(qb[s], xt[-Ns + (s / 3 - 1) * Mx + (s % 3 - 1)], acc);
+          }
+        }
+        if (o32) acc = fmaf(o32[k], xt[0], acc);
+        y[k] = acc;
+        dot = fmaf(xt[0], acc, dot);
+      }
+    }
+  }
+  const double bs = block_sum(dot, red);
+  if (threadIdx.x == 0) part[int64_t(col) * gridDim.x + blockIdx.x] = bs;
+}
+
+// Diagonal of A at node (cell c, time t) from the FP32 coefficients
+__device__ __forceinline__ float diag32(const float* __restrict__ cf, int Ns, int T, int sep, float qe, float qm,
+                                        int c, int t) {
+  if (sep) return (t == 0 || t == T - 1 ? qe : qm) * cf[int64_t(25 + 12) * Ns + c];
+  if (T == 1) return cf[int64_t(25 + 12) * Ns + c];
+  if (t == 0) return cf[int64_t(12) * Ns + c] + cf[int64_t(68) * Ns + c];
+  return cf[int64_t(25 + 12) * Ns + c] + (t < T - 1 ? cf[int64_t(68) * Ns + c] : 0.f);
+}
+
+// Elementwise step of column blockIdx.y (grid-stride over the nodes):
+//   xc += alpha p, r -= alpha Ap   (alpha 0: no update)
+//   mode 0: z = r;  mode 1: z = r / A_pp;  mode 2: z left to the G^T G kernel
+// and the block's partial sums of r . z (mode < 2) into partA[col G + b] and of
+// r . r into partB[col G + b].
+constexpr int kElemBlocks = 1216;  // 8 per SM
+__global__ void __launch_bounds__(256) update32c_kernel(int Ns, int T, int sep, float qe, float qm, int mode,
+                                                        const float* __restrict__ cf, const float* __restrict__ o32,
+                                                        float* __restrict__ xc, float* __restrict__ rv,
+                                                        const float* __restrict__ pv, const float* __restrict__ apv,
+                                                        float* __restrict__ zv, const float* __restrict__ alpha,
+                                                        double* __restrict__ partA, double* __restrict__ partB) {
+  __shared__ float red[8];
+  const int64_t n = int64_t(Ns) * T;
+  const int col = blockIdx.y;
+  const float a = alpha[col];
+  float* r = rv + col * n;
+  float srz = 0.f, srr = 0.f;
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += int64_t(gridDim.x) * blockDim.x) {
+    float rk = r[k];
+    if (a != 0.f) {
+      xc[col * n + k] = fmaf(a, pv[col * n + k], xc[col * n + k]);
+      rk = fmaf(-a, apv[col * n + k], rk);
+      r[k] = rk;
+    }
+    srr = fmaf(rk, rk, srr);
+    if (mode < 2) {
+      float zk = rk;
+      if (mode == 1) {
+        const int t = int(k / Ns), c = int(k - int64_t(t) * Ns);
+        zk = __fdividef(rk, diag32(cf, Ns, T, sep, qe, qm, c, t) + (o32 ? o32[k] : 0.f));
+      }
+      zv[col * n + k] = zk;
+      srz = fmaf(rk, zk, srz);
+    }
+  }
+  const double b1 = block_sum(srz, red);
+  if (threadIdx.x == 0 && mode < 2) partA[int64_t(col) * gridDim.x + blockIdx.x] = b1;
+  const double b2 = block_sum(srr, red);
+  if (threadIdx.x == 0) partB[int64_t(col) * gridDim.x + blockIdx.x] = b2;
+}
+
+// Row o of G at node q (time t, cell c): the row's start and stride in the
+// weight array (compact: class row or observed row; else the per-node layout)
+struct GWeights {
+  const float* w;
+  const uint32_t* mask;  // compact, with observations: observed nodes have their own rows
+  const int* rank;
+  int nob, Ns, T, compact;
+  __device__ __forceinline__ void row(int q, int t, int c, int64_t* base, int* stride) const {
+    if (!compact) { *base = q; *stride = Ns * T; return; }
+    if (mask) {
+      const uint32_t m = mask[q >> 5], bit = 1u << (q & 31);
+      if (m & bit) {
+        *base = int64_t(3) * kOff * Ns + rank[q >> 5] + __popc(m & (bit - 1u));
+        *stride = nob;
+        return;
+      }
+    }
+    const int k = T == 1 || t == 0 ? 0 : (t == T - 1 ? 2 : 1);
+    *base = int64_t(k) * kOff * Ns + c;
+    *stride = Ns;
+  }
+};
+
+// z = G^T G r for column blockIdx.z, one block per 32 x 8 tile of cells and
+// chunk of kGtgT time steps, and the block's partial sum of r . z.  The block
+// stages r (halo 2) and u = G r (halo 1) for three time slices in shared
+// memory, sweeping the time axis, so r is read once and u never leaves the
+// chip; the rows of G come from L1 / L2.
+constexpr int kGX = 32, kGY = 8, kGtgT = 12;
+constexpr int kRX = kGX + 4, kRY = kGY + 4, kUX = kGX + 2, kUY = kGY + 2;
+__global__ void __launch_bounds__(256) gtg32c_kernel(int Mx, int Ny, int T, GWeights gw,
+                                                     const float* __restrict__ rv, float* __restrict__ zv,
+                                                     double* __restrict__ part) {
+  __shared__ float R[3][kRY][kRX];
+  __shared__ float U[3][kUY][kUX];
+  __shared__ int UB[3][kUY][kUX];    // row start of G at the u node (-1: outside the grid)
+  __shared__ int US[3][kUY][kUX];    // its stride
+  __shared__ float red[8];
+  const int Ns = Mx * Ny;
+  const int64_t n = int64_t(Ns) * T;
+  const int col = blockIdx.z;
+  const float* r = rv + col * n;
+  float* z = zv + col * n;
+  const int ntx = (Mx + kGX - 1) / kGX;
+  const int x0 = (blockIdx.x % ntx) * kGX, y0 = (blockIdx.x / ntx) * kGY;
+  const int t0 = blockIdx.y * kGtgT, t1 = min(T, t0 + kGtgT);
+  const int tid = threadIdx.x;
+  float rz = 0.f;
+  for (int s = t0 - 2; s <= t1 + 1; ++s) {
+    // (a) r at time s, cells with halo 2
+    if (s >= 0 && s < T) {
+      float* Rs = &R[(s + 3) % 3][0][0];
+      for (int i = tid; i < kRY * kRX; i += 256) {
+        const int yy = y0 - 2 + i / kRX, xx = x0 - 2 + i % kRX;
+        Rs[i] = (xx >= 0 && xx < Mx && yy >= 0 && yy < Ny) ? r[int64_t(s) * Ns + yy * Mx + xx] : 0.f;
+      }
+    }
+    __syncthreads();
+    // (b) u = G r at time s - 1, cells with halo 1
+    const int tu = s - 1;
+    if (tu >= t0 - 1 && tu <= t1 && tu >= 0 && tu < T) {
+      const int su = (tu + 3) % 3;
+      for (int i = tid; i < kUY * kUX; i += 256) {
+        const int ly = i / kUX, lx = i % kUX;
+        const int yy = y0 - 1 + ly, xx = x0 - 1 + lx;
+        float u = 0.f;
+        int rb = -1, rs = 0;
+        if (xx >= 0 && xx < Mx && yy >= 0 && yy < Ny) {
+          const int c = yy * Mx + xx;
+          int64_t b64;
+          gw.row(tu * Ns + c, tu, c, &b64, &rs);
+          rb = int(b64);
+#pragma unroll
+          for (int o = 0; o < kOff; ++o) {
+            const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+            const int tr = tu + dt;
+            if (tr < 0 || tr >= T) continue;
+            u = fmaf(gw.w[b64 + int64_t(o) * rs], R[(tr + 3) % 3][ly + 1 + dy][lx + 1 + dx], u);
+          }
+        }
+        U[su][ly][lx] = u;
+        UB[su][ly][lx] = rb;
+        US[su][ly][lx] = rs;
+      }
+    }
+    __syncthreads();
+    // (c) z = G^T u at time s - 2, this block's cells
+    const int tz = s - 2;
+    if (tz >= t0 && tz < t1) {
+      const int ly = tid / kGX, lx = tid % kGX;
+      const int yy = y0 + ly, xx = x0 + lx;
+      if (xx < Mx && yy < Ny) {
+        float acc = 0.f;
+#pragma unroll
+        for (int o = 0; o < kOff; ++o) {
+          const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+          const int tq = tz - dt;  // node q = p - o holds row o's weight for p
+          if (tq < 0 || tq >= T) continue;
+          const int sq = (tq + 3) % 3, qy = ly + 1 - dy, qx = lx + 1 - dx;
+          const int rb = UB[sq][qy][qx];
+          if (rb < 0) continue;
+          acc = fmaf(gw.w[int64_t(rb) + int64_t(o) * US[sq][qy][qx]], U[sq][qy][qx], acc);
+        }
+        const int64_t k = int64_t(tz) * Ns + yy * Mx + xx;
+        z[k] = acc;
+        rz = fmaf(R[(tz + 3) % 3][ly + 2][lx + 2], acc, rz);
+      }
+    }
+    __syncthreads();
+  }
+  const double bs = block_sum(rz, red);
+  if (threadIdx.x == 0)
+    part[int64_t(col) * gridDim.x * gridDim.y + blockIdx.y * gridDim.x + blockIdx.x] = bs;
+}
+
+// Per-column scalars from block partials (one block per column, fixed order):
+//   mode 0: pap = sum partA;  alpha = rz / pap (0 if done or pap <= 0)
+//   mode 1: rzn = sum partA, rr = sum partB;  beta = rzn / rz, rz = rzn
+//   mode 2: rz = sum partA, rr = sum partB, beta = 0 (a new or replaced residual)
+__global__ void scal32_kernel(const double* __restrict__ partA, int na, const double* __restrict__ partB, int nb,
+                              int mode, const int* __restrict__ done, double* __restrict__ rz,
+                              double* __restrict__ rr, double* __restrict__ pap, float* __restrict__ alpha,
+                              float* __restrict__ beta) {
+  __shared__ double sh[2][256];
+  const int col = blockIdx.x;
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = threadIdx.x; i < na; i += 256) s1 += partA[int64_t(col) * na + i];
+  if (mode != 0)
+    for (int i = threadIdx.x; i < nb; i += 256) s2 += partB[int64_t(col) * nb + i];
+  sh[0][threadIdx.x] = s1;
+  sh[1][threadIdx.x] = s2;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if (threadIdx.x < k) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + k];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double a = sh[0][0], b = sh[1][0];
+  if (mode == 0) {
+    pap[col] = a;
+    alpha[col] = (!done[col] && a > 0.0) ? float(rz[col] / a) : 0.f;
+  } else if (mode == 1) {
+    beta[col] = (!done[col] && rz[col] != 0.0) ? float(a / rz[col]) : 0.f;
+    rz[col] = a;
+    rr[col] = b;
+  } else {
+    rz[col] = a;
+    rr[col] = b;
+    beta[col] = 0.f;
+  }
+}
+
+//   p = z + beta p (finished columns unchanged)
+__global__ void p32c_kernel(float* __restrict__ pv, const float* __restrict__ zv, const float* __restrict__ beta,
+                            const int* __restrict__ done, int64_t n) {
+  const int col = blockIdx.y;
+  if (done[col]) return;
+  const float b = beta[col];
+  for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < n; k += int64_t(gridDim.x) * blockDim.x)
+    pv[col * n + k] = fmaf(b, pv[col * n + k], zv[col * n + k]);
 }
 
 }  // namespace
@@ -561,65 +923,181 @@ int jacobi_smooth(Plan* p, int with_obs, double tau, double omega, int sweeps, d
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+float* scratch32(Plan* p, size_t elems) {
+  if (elems > p->pc32_cap) {
+    cudaFree(p->d_pc32);
+    p->d_pc32 = nullptr;
+    p->pc32_cap = 0;
+    if (cudaMalloc(&p->d_pc32, elems * sizeof(float)) != cudaSuccess) return nullptr;
+    p->pc32_cap = elems;
+  }
+  return static_cast<float*>(p->d_pc32);
+}
+
+// Compact weights start with a 4-int header (magic, observed rows included,
+// observation-set version, number of observed rows) so that a solve can check
+// that they belong to its observation set; the rows follow.
+constexpr int kCompactHeader = 4;
+constexpr int kCompactMagic = 0x53504345;
+
+int64_t pc_compact_floats(const Plan* p) {
+  return kCompactHeader + int64_t(kOff) * (3 * int64_t(p->sym.Mx) * p->sym.Ny + p->nob);
+}
+
+int pc_weights_compact(Plan* p, int with_obs, double tau, const float* prm, float* w) {
+  const int Ns = p->sym.Mx * p->sym.Ny;
+  const int nob = with_obs ? p->nob : 0;
+  const int64_t rows = 3 * int64_t(Ns) + nob;
+  static thread_local int head[kCompactHeader];
+  head[0] = kCompactMagic;
+  head[1] = with_obs ? 1 : 0;
+  head[2] = p->obs_version;
+  head[3] = nob;
+  cudaMemcpyAsync(w, head, sizeof(head), cudaMemcpyHostToDevice, p->stream);
+  pc_forward_compact_kernel<<<nblk(rows, 128), 128, 0, p->stream>>>(p->qstencil(), with_obs ? p->d_obs_cnt : nullptr,
+                                                                    tau, p->d_obs_nodes, nob, prm,
+                                                                    w + kCompactHeader);
+  // the header copy reads host memory asynchronously: finish before it can change
+  return cudaStreamSynchronize(p->stream) == cudaSuccess && cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+// Reliable-update PCG: the recursive FP32 residual is replaced by the true
+// FP64 one (and the FP32 correction added into the FP64 solution) whenever it
+// has fallen by this factor since the last replacement, reaches the tolerance,
+// or kReplaceEvery iterations have passed.
+constexpr double kReplaceDrop = 0.1;
+constexpr int kReplaceEvery = 64;
+
 int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const double* b, double* x, int nrhs,
               double tol, int maxit, int check_every, int* iters, double* relres) {
   const int64_t n = p->sym.n, len = n * nrhs;
-  if (len >= (int64_t(1) << 31)) return 1;  // the stencil kernels index entries in 32 bits
-  const size_t need = size_t(5 * len) + size_t(kDotBlocks) * nrhs + size_t(8 * nrhs) + size_t(nrhs);
-  double* base = scratch(p, need);
-  if (!base) return 4;
-  double *r = base, *z = r + len, *pp = z + len, *ap = pp + len, *tmp = ap + len, *part = tmp + len;
-  double* sc = part + size_t(kDotBlocks) * nrhs;  // rz, rzn, pap, rr, bb (nrhs each)
-  double *rz = sc, *rzn = sc + nrhs, *pap = sc + 2 * nrhs, *rr = sc + 3 * nrhs, *bb = sc + 4 * nrhs;
+  if (len >= (int64_t(1) << 31) || nrhs > 65535) return 1;  // the stencil kernels index in 32 bits
+  const int Mx = p->sym.Mx, Ny = p->sym.Ny, Ns = Mx * Ny, T = p->sym.T;
+  cudaStream_t st = p->stream;
+  const int nch = (T + kTch - 1) / kTch;
+  const int nsp = nblk(int64_t(Ns) * nch, 128);
+  const int ntiles = ((Mx + kGX - 1) / kGX) * ((Ny + kGY - 1) / kGY), ngch = (T + kGtgT - 1) / kGtgT;
+  const int ngtg = ntiles * ngch;
+  const int na_max = std::max(nsp, std::max(int(kElemBlocks), ngtg));
+  // FP64: true residual (row-major), block partials, per-column scalars
+  const size_t need64 = size_t(len) + size_t(nrhs) * (na_max + kElemBlocks) + size_t(kDotBlocks) * nrhs +
+                        size_t(8 * nrhs) + size_t(nrhs);
+  double* base = scratch(p, need64);
+  // FP32 (column-major): r, z, p, Ap, x correction; coefficients; observation term; alpha, beta
+  const size_t need32 = size_t(5 * len) + size_t(kCoef32) * Ns + size_t(n) + size_t(2 * nrhs);
+  float* b32 = scratch32(p, need32);
+  if (!base || !b32) return 4;
+  double* r64 = base;
+  double* partA = r64 + len;
+  double* partB = partA + size_t(nrhs) * na_max;
+  double* part64 = partB + size_t(nrhs) * kElemBlocks;
+  double* sc = part64 + size_t(kDotBlocks) * nrhs;
+  double *rz = sc, *pap = sc + nrhs, *rr = sc + 2 * nrhs, *bb = sc + 3 * nrhs, *rrt = sc + 4 * nrhs;
   int* done = reinterpret_cast<int*>(sc + 8 * nrhs);
+  float *r32 = b32, *z32 = r32 + len, *p32 = z32 + len, *ap32 = p32 + len, *xc32 = ap32 + len;
+  float* cf = xc32 + len;
+  float* o32 = cf + size_t(kCoef32) * Ns;
+  float* alpha = o32 + n;
+  float* beta = alpha + nrhs;
   const QStencil q = p->qstencil();
   const double* obs = with_obs ? p->d_obs_cnt : nullptr;
-  cudaStream_t st = p->stream;
+  const int sep = q.sep;
+  const float qe = float(q.qt_end), qm = float(q.qt_mid), qo = float(q.qt_off);
+  const int mode = kind == 0 ? 0 : (kind == 1 ? 1 : 2);
+  if (kind == 3) {
+    // compact weights hold observed rows for the observation set they were computed with
+    int head[kCompactHeader] = {0, 0, 0, 0};
+    if (cudaMemcpyAsync(head, w, sizeof(head), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return 2;
+    const bool ok = head[0] == kCompactMagic && head[1] == (with_obs ? 1 : 0) &&
+                    (!with_obs || (head[2] == p->obs_version && head[3] == p->nob));
+    if (!ok) return 7;
+    w += kCompactHeader;
+  }
+  GWeights gw{w, (kind == 3 && with_obs) ? p->d_obs_mask : nullptr, p->d_obs_rank, p->nob, Ns, T, kind == 3 ? 1 : 0};
+  coef32_kernel<<<nblk(Ns, 128), 128, 0, st>>>(q, cf);
+  if (obs) obs32_kernel<<<nblk(n), 256, 0, st>>>(obs, tau, o32, n);
+  const float* o = obs ? o32 : nullptr;
+  const dim3 gsp(nsp, nrhs), gel(kElemBlocks, nrhs), ggt(ntiles, ngch, nrhs);
+  // z = M r with the partial sums of r . z and r . r, after the update of r by alpha
+  auto update_precond = [&]() {
+    update32c_kernel<<<gel, 256, 0, st>>>(Ns, T, sep, qe, qm, mode, cf, o, xc32, r32, p32, ap32, z32, alpha, partA,
+                                          partB);
+    if (mode == 2) gtg32c_kernel<<<ggt, 256, 0, st>>>(Mx, Ny, T, gw, r32, z32, partA);
+  };
+  const int na = mode == 2 ? ngtg : int(kElemBlocks);
+  // a new residual r32: z = M r, rz = r . z (p unchanged)
+  auto restart = [&]() {
+    cudaMemsetAsync(alpha, 0, size_t(nrhs) * sizeof(float), st);
+    update_precond();
+    scal32_kernel<<<nrhs, 256, 0, st>>>(partA, na, partB, kElemBlocks, 2, done, rz, rr, pap, alpha, beta);
+  };
+  auto true_residual = [&]() {
+    launch_spmv(q, obs, tau, x, r64, nrhs, st);
+    pc_sub_kernel<<<nblk(len), 256, 0, st>>>(b, r64, len);
+    col_dots(p, r64, r64, nrhs, part64, rrt);
+  };
   cudaMemsetAsync(x, 0, size_t(len) * sizeof(double), st);
-  cudaMemcpyAsync(r, b, size_t(len) * sizeof(double), cudaMemcpyDeviceToDevice, st);
-  cudaMemsetAsync(done, 0, size_t(nrhs) * sizeof(int), st);
-  col_dots(p, b, b, nrhs, part, bb);
-  apply_precond(p, kind, w, obs, tau, r, z, tmp, nrhs);
-  cudaMemcpyAsync(pp, z, size_t(len) * sizeof(double), cudaMemcpyDeviceToDevice, st);
-  col_dots(p, r, z, nrhs, part, rz);
-  std::vector<double> hb(nrhs), hr(nrhs);
+  cudaMemsetAsync(xc32, 0, size_t(len) * sizeof(float), st);
+  cudaMemsetAsync(p32, 0, size_t(len) * sizeof(float), st);
+  col_dots(p, b, b, nrhs, part64, bb);
+  std::vector<double> hb(nrhs), hr(nrhs), href(nrhs);
   std::vector<int> hd(nrhs, 0);
   cudaMemcpyAsync(hb.data(), bb, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return 2;
-  int it = 0;
-  double worst = 0.0;
-  bool all_done = false;
+  for (int c = 0; c < nrhs; ++c)
+    if (!(hb[c] > 0.0)) hd[c] = 1;  // a zero right-hand side is solved by x = 0
+  cudaMemcpyAsync(done, hd.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, st);
+  href = hb;
+  to32cm_kernel<<<nblk(len), 256, 0, st>>>(b, r32, n, nrhs);
+  restart();
+  p32c_kernel<<<gel, 256, 0, st>>>(p32, z32, beta, done, n);  // p = z
+  const double tol2 = tol * tol;
+  const int every = std::max(1, std::min(check_every, 4));
+  int it = 0, last_rep = 0;
+  bool all_done = false, fresh = false;  // fresh: x holds every correction and rrt is its true residual
+  for (int c = 0; c < nrhs; ++c) all_done = (c == 0 || all_done) && hd[c];
   while (it < maxit && !all_done) {
-    launch_spmv(q, obs, tau, pp, ap, nrhs, st);
-    col_dots(p, pp, ap, nrhs, part, pap);
-    pcg_xr_kernel<<<nblk(len), 256, 0, st>>>(x, r, pp, ap, rz, pap, done, n, nrhs);
-    apply_precond(p, kind, w, obs, tau, r, z, tmp, nrhs);
-    col_dots(p, r, z, nrhs, part, rzn);
-    pcg_p_kernel<<<nblk(len), 256, 0, st>>>(pp, z, rzn, rz, done, n, nrhs);
-    cudaMemcpyAsync(rz, rzn, nrhs * sizeof(double), cudaMemcpyDeviceToDevice, st);
+    spmv32c_kernel<<<gsp, 128, 0, st>>>(Mx, Ny, T, sep, qe, qm, qo, cf, o, p32, ap32, partA);
+    scal32_kernel<<<nrhs, 256, 0, st>>>(partA, nsp, partB, 0, 0, done, rz, rr, pap, alpha, beta);
+    update_precond();
+    scal32_kernel<<<nrhs, 256, 0, st>>>(partA, na, partB, kElemBlocks, 1, done, rz, rr, pap, alpha, beta);
+    p32c_kernel<<<gel, 256, 0, st>>>(p32, z32, beta, done, n);
     ++it;
-    if (it % check_every == 0 || it == maxit) {
-      col_dots(p, r, r, nrhs, part, rr);
-      cudaMemcpyAsync(hr.data(), rr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st);
-      if (cudaStreamSynchronize(st) != cudaSuccess) return 2;
-      all_done = true;
-      worst = 0.0;
-      for (int c = 0; c < nrhs; ++c) {
-        const double rel = hb[c] > 0.0 ? sqrt(hr[c] / hb[c]) : 0.0;
-        if (!hd[c] && rel <= tol) hd[c] = 1;
-        all_done = all_done && hd[c];
-        worst = std::max(worst, rel);
-      }
-      cudaMemcpyAsync(done, hd.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, st);
+    fresh = false;
+    if (it % every != 0 && it != maxit) continue;
+    cudaMemcpyAsync(hr.data(), rr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 2;
+    bool replace = it == maxit || it - last_rep >= kReplaceEvery;
+    for (int c = 0; c < nrhs && !replace; ++c)
+      if (!hd[c] && (hr[c] <= kReplaceDrop * kReplaceDrop * href[c] || hr[c] <= tol2 * hb[c])) replace = true;
+    if (!replace) continue;
+    acc64cm_kernel<<<nblk(len), 256, 0, st>>>(x, xc32, n, nrhs);
+    true_residual();
+    cudaMemcpyAsync(hr.data(), rrt, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 2;
+    fresh = true;
+    last_rep = it;
+    all_done = true;
+    for (int c = 0; c < nrhs; ++c) {
+      if (!hd[c] && hr[c] <= tol2 * hb[c]) hd[c] = 1;
+      all_done = all_done && hd[c];
+      href[c] = hr[c];
     }
+    if (all_done) break;
+    cudaMemcpyAsync(done, hd.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, st);
+    // continue from the true residual (p kept)
+    to32cm_kernel<<<nblk(len), 256, 0, st>>>(r64, r32, n, nrhs);
+    restart();
   }
-  // true residual of the returned x
-  launch_spmv(q, obs, tau, x, ap, nrhs, st);
-  pc_sub_kernel<<<nblk(len), 256, 0, st>>>(b, ap, len);
-  col_dots(p, ap, ap, nrhs, part, rr);
-  cudaMemcpyAsync(hr.data(), rr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) return 2;
-  worst = 0.0;
+  if (!fresh) {
+    acc64cm_kernel<<<nblk(len), 256, 0, st>>>(x, xc32, n, nrhs);
+    true_residual();
+    cudaMemcpyAsync(hr.data(), rrt, nrhs * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 2;
+  }
+  double worst = 0.0;
   for (int c = 0; c < nrhs; ++c) worst = std::max(worst, hb[c] > 0.0 ? sqrt(hr[c] / hb[c]) : 0.0);
   *iters = it;
   *relres = worst;

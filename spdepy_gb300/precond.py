@@ -48,8 +48,12 @@ class LearnedPreconditioner:
         self.params = torch.as_tensor(p).cuda().contiguous()
         self.history = []
 
-    def weights(self, plan, with_obs=False, tau=0.0):
-        """Stencil weights of G for the system currently assembled on `plan`."""
+    def weights(self, plan, with_obs=False, tau=0.0, compact=True):
+        """Stencil weights of G for the system currently assembled on `plan`: by
+        default the compact form (rows per cell and time class, and per observed
+        node), else one row per node."""
+        if compact:
+            return plan.precond_weights_compact(self.params, with_obs, tau)
         return plan.precond_weights(self.params, with_obs, tau)[0]
 
     def train(self, make_system, steps, probes=4, lr=3e-3, seed=0, smooth=2, sweeps=20):

@@ -228,6 +228,16 @@ class GPUPlan:
                                                  None if act is None else act.data_ptr()), self._h, "precond_weights")
         return w, act
 
+    def precond_weights_compact(self, params, with_obs=False, tau=0.0):
+        """G's rows once per (cell, time class) and per observed node (spde_precond_weights_compact)."""
+        torch = _torch()
+        size = ctypes.c_int64()
+        nat.check(nat.lib().spde_precond_compact_size(self._h, ctypes.byref(size)), self._h, "precond_compact_size")
+        w = torch.empty(max(int(size.value), 1), dtype=torch.float32, device="cuda")
+        nat.check(nat.lib().spde_precond_weights_compact(self._h, int(with_obs), float(tau), params.data_ptr(),
+                                                         w.data_ptr()), self._h, "precond_weights_compact")
+        return CompactWeights(w)
+
     def precond_grad(self, params, w, act, z, with_obs=False, tau=0.0):
         torch = _torch()
         z = z.to(device="cuda", dtype=torch.float64).contiguous()
@@ -261,12 +271,15 @@ class GPUPlan:
         return z
 
     def pcg(self, b, with_obs=False, tau=0.0, precond="jacobi", w=None, tol=1e-8, maxit=20000, check=True):
-        """x = A^-1 b by preconditioned CG; precond "none", "jacobi" or "learned" (w)."""
+        """x = A^-1 b by preconditioned CG; precond "none", "jacobi" or "learned" (w: per-node
+        weights, or the CompactWeights of precond_weights_compact)."""
         torch = _torch()
         b = b.to(device="cuda", dtype=torch.float64).contiguous()
         nrhs = 1 if b.dim() == 1 else b.shape[1]
         x = torch.empty_like(b)
         kind = {"none": 0, "jacobi": 1, "learned": 2}[precond]
+        if kind == 2 and isinstance(w, CompactWeights):
+            kind, w = 3, w.data
         it, rel = ctypes.c_int(), ctypes.c_double()
         rc = nat.lib().spde_pcg(self._h, int(with_obs), float(tau), kind, None if w is None else w.data_ptr(),
                                 b.data_ptr(), x.data_ptr(), nrhs, float(tol), int(maxit), ctypes.byref(it),
@@ -292,6 +305,17 @@ class GPUPlan:
         nat.check(nat.lib().spde_loglike(self._h, canon.ctypes.data, canon.size, y.data_ptr(), r, grad_mode, pp, nh1,
                                          ctypes.byref(f), jac.ctypes.data), self._h, "loglike")
         return f.value, jac
+
+
+class CompactWeights:
+    """Compact learned-preconditioner weights (one row of G per cell and time
+    class, and per observed node), for SPDE_PRECOND_LEARNED_COMPACT."""
+
+    def __init__(self, data):
+        self.data = data
+
+    def data_ptr(self):
+        return self.data.data_ptr()
 
 
 class PrecisionQ:
@@ -611,9 +635,9 @@ class SpdeModel:
         if isinstance(precond, str):
             kind = {"none": 0, "jacobi": 1}[precond]
         else:
-            kind = 2
             wq = precond.weights(plan, False, 0.0)
             wqc = precond.weights(plan, True, tau)
+            kind = 3 if isinstance(wq, CompactWeights) else 2
         jac = np.zeros(canon.size)
         it = ctypes.c_int()
         nat.check(nat.lib().spde_loglike_grad_pcg(plan.h, tau, y.data_ptr(), self.r, V.data_ptr(), nh1, kind,

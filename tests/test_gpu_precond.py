@@ -161,3 +161,35 @@ def test_posterior_draws_by_pcg_match_cholesky():
     xs, _ = plan.solve(rhs)
     ref = (xs + mu[:, None]).cpu().numpy()
     np.testing.assert_allclose(x_pcg.cpu().numpy(), ref, rtol=0, atol=1e-9 * np.abs(ref).max())
+
+
+def test_compact_weights_are_the_per_node_operator():
+    """The compact weights (one row of G per cell and time class, one per observed
+    node) expand to exactly the per-node weights, PCG gives the same solution
+    with either, and a solve with another observation setting is refused."""
+    import spdepy_gb300._native as nat
+    from spdepy_gb300.precond import LearnedPreconditioner
+    g, mod, tau = _golden_system()
+    plan, grid = mod.plan, mod.grid
+    lp = LearnedPreconditioner(seed=3)
+    lp.params.add_(torch.randn(lp.params.shape, generator=torch.Generator().manual_seed(4)).cuda() * 0.05)
+    wn = lp.weights(plan, True, tau, compact=False).view(27, grid.n).cpu().numpy()
+    wc = lp.weights(plan, True, tau)
+    raw = wc.data.cpu().numpy()
+    n, Ns, T = grid.n, grid.Mx * grid.Ny, grid.T
+    obs_nodes = np.unique(grid.obs_nodes(g["idx"]))
+    cls = raw[4:4 + 3 * 27 * Ns].reshape(3, 27, Ns)
+    orow = raw[4 + 3 * 27 * Ns:].reshape(27, obs_nodes.size)
+    k = np.arange(n)
+    t, c = np.divmod(k, Ns)
+    klass = np.where(t == 0, 0, np.where(t == T - 1, 2, 1))
+    full = cls[klass, :, c].T.copy()
+    full[:, obs_nodes] = orow
+    np.testing.assert_array_equal(full, wn)
+    b = torch.as_tensor(np.random.default_rng(2).normal(size=(grid.n, 3)))
+    x1, it1, r1 = plan.pcg(b, True, tau, "learned", w=torch.as_tensor(wn.ravel()).cuda(), tol=1e-10)
+    x2, it2, r2 = plan.pcg(b, True, tau, "learned", w=wc, tol=1e-10)
+    assert r1 <= 1e-10 and r2 <= 1e-10 and abs(it1 - it2) <= 4
+    np.testing.assert_allclose(x2.cpu().numpy(), x1.cpu().numpy(), rtol=0, atol=1e-8 * np.abs(x1.cpu().numpy()).max())
+    with pytest.raises(nat.SpdeError, match="do not match"):
+        plan.pcg(b, False, 0.0, "learned", w=wc, tol=1e-8)
