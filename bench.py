@@ -205,7 +205,7 @@ def cpu_baseline(n_full, passes=1):
     return _cpu_figures(points, n_full, passes)
 
 
-def learned_pcg_leg(train_steps=5000):
+def learned_pcg_leg(train_steps=5000, size=(400, 400, 48)):
     """Conditional-mean solve by PCG on the 400 x 400 x 48 non-stationary
     workload (7.68M nodes, seed 2, 1 % observed, right-hand side tau S^T y with
     synthetic y ~ N(0, 1)) with the learned preconditioner trained on
@@ -222,7 +222,7 @@ def learned_pcg_leg(train_steps=5000):
     hist = lp.train(system_maker(wt, mt), steps=train_steps, probes=4, lr=3e-3, seed=1)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
-    we = nonstationary_advection_diffusion(M=400, N=400, T=48, seed=2)
+    we = nonstationary_advection_diffusion(M=size[0], N=size[1], T=size[2], seed=2)
     me = build_model(we, "iterative")
     me._assemble(we.par)
     rng = np.random.default_rng(2)
@@ -233,7 +233,7 @@ def learned_pcg_leg(train_steps=5000):
     b = np.zeros(n)
     b[idx] = tau * rng.normal(size=idx.size)
     bt = torch.as_tensor(b).cuda()
-    out = {"workload": f"nonstationary advection-diffusion 400x400x48 ({n} nodes), seed 2, 1% observed",
+    out = {"workload": f"nonstationary advection-diffusion {size[0]}x{size[1]}x{size[2]} ({n} nodes), seed 2, 1% observed",
            "tol": 1e-6,
            "training": {"systems": train_steps, "grid": "100x100x12", "probes_per_system": 4,
                         "seconds": round(t_train, 2), "loss_first10": float(np.mean(hist[:10])),
@@ -415,6 +415,9 @@ def main():
                     help="timed evaluations of the plain FP64 plan (the metric's denominator); 0 skips it")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-pcg", action="store_true")
+    ap.add_argument("--pcg-only", action="store_true", help="run only the learned-PCG leg and print its record")
+    ap.add_argument("--pcg-train-steps", type=int, default=5000)
+    ap.add_argument("--pcg-size", default="400,400,48")
     ap.add_argument("--fit", action="store_true", help="also run the L-BFGS fit on the sensor-track workload")
     ap.add_argument("--no-config2", action="store_true",
                     help="skip the mixed-vs-FP64 comparison on the stationary 100x100x24 model")
@@ -427,6 +430,12 @@ def main():
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.pcg_only:
+        from spdepy_gb300 import build as b
+        b.build()
+        size = tuple(int(v) for v in args.pcg_size.split(","))
+        print(json.dumps({"learned_pcg": learned_pcg_leg(args.pcg_train_steps, size)}))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -553,7 +562,7 @@ def main():
     if rank != 0:
         return
     cb = None if (args.no_cpu or world > 1) else cpu_baseline(w.grid.n)  # rank 0 at N = 1 only
-    pcg = None if args.no_pcg else learned_pcg_leg()
+    pcg = None if args.no_pcg else learned_pcg_leg(args.pcg_train_steps)
     fit = lbfgs_fit_leg() if args.fit else None
     c2 = None if args.no_config2 else config2_leg()
     nobs = int(w.idx.size)

@@ -521,99 +521,67 @@ __device__ __forceinline__ double block_sum(float v, float* red) {
   return s;
 }
 
-// Time steps per thread of the stencil product (more threads than one per cell)
-constexpr int kTch = 8;
-
-// ap = A p in FP32 for column blockIdx.y; one thread per (cell, chunk of kTch
-// time steps), and the block's partial sum of p . ap into part[col gridDim.x + block]
-__global__ void __launch_bounds__(128) spmv32c_kernel(int Mx, int Ny, int T, int sep, float qe, float qm, float qo,
-                                                      const float* __restrict__ cf, const float* __restrict__ o32,
-                                                      const float* __restrict__ pv, float* __restrict__ apv,
-                                                      double* __restrict__ part) {
-  __shared__ float red[4];
-  const int Ns = Mx * Ny;
-  const int64_t n = int64_t(Ns) * T;
+// ap = A p in FP32 for column blockIdx.y, one thread per node (the cell's
+// coefficients, shared by all its time steps, come from L1 / L2), and the
+// block's partial sum of p . ap into part[col gridDim.x + block].  Node and
+// coefficient offsets fit in 32 bits (checked by the caller).
+__global__ void __launch_bounds__(256, 4) spmv32n_kernel(int Mx, int Ny, int T, int sep, float qe, float qm,
+                                                         float qo, const float* __restrict__ cf,
+                                                         const float* __restrict__ o32, const float* __restrict__ pv,
+                                                         float* __restrict__ apv, double* __restrict__ part) {
+  __shared__ float red[8];
+  const int Ns = Mx * Ny, n = Ns * T;
   const int col = blockIdx.y;
-  const float* x = pv + col * n;
-  float* y = apv + col * n;
-  const int nch = (T + kTch - 1) / kTch;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const float* x = pv + int64_t(col) * n;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   float dot = 0.f;
-  if (e < Ns * nch) {
-    const int j = e / Ns, c = e - j * Ns;
+  if (k < n) {
+    const int t = k / Ns, c = k - t * Ns;
     const int cy = c / Mx, cx = c - cy * Mx;
-    const int t0 = j * kTch, t1 = min(T, t0 + kTch);
-    float qa[25];
-    uint32_t m25 = 0, m9 = 0;
-#pragma unroll
-    for (int s = 0; s < 25; ++s) {
-      const int dx = s % 5 - 2, dy = s / 5 - 2;
-      m25 |= uint32_t(cx + dx >= 0 && cx + dx < Mx && cy + dy >= 0 && cy + dy < Ny) << s;
-      qa[s] = cf[int64_t(25 + s) * Ns + c];
-    }
-#pragma unroll
-    for (int s = 0; s < 9; ++s) {
-      const int dx = s % 3 - 1, dy = s / 3 - 1;
-      m9 |= uint32_t(cx + dx >= 0 && cx + dx < Mx && cy + dy >= 0 && cy + dy < Ny) << s;
-    }
-    auto spatial = [&](const float* xt) {
+    // bit (dx + 2) of vx: cx + dx inside the grid; likewise vy
+    const uint32_t vx = (cx >= 2 ? 1u : 0u) | (cx >= 1 ? 2u : 0u) | 4u | (cx + 1 < Mx ? 8u : 0u) | (cx + 2 < Mx ? 16u : 0u);
+    const uint32_t vy = (cy >= 2 ? 1u : 0u) | (cy >= 1 ? 2u : 0u) | 4u | (cy + 1 < Ny ? 8u : 0u) | (cy + 2 < Ny ? 16u : 0u);
+    const float* cc = cf + c;
+    const float* xt = x + k;
+    const int sb = (t == 0 && T > 1 && !sep) ? 0 : 25;
+    auto block25 = [&](const float* xs) {
       float acc = 0.f;
 #pragma unroll
-      for (int s = 0; s < 25; ++s)
-        if (m25 >> s & 1u) acc = fmaf(qa[s], xt[(s / 5 - 2) * Mx + (s % 5 - 2)], acc);
+      for (int s = 0; s < 25; ++s) {
+        const int dx = s % 5 - 2, dy = s / 5 - 2;
+        if ((vx >> (dx + 2)) & (vy >> (dy + 2)) & 1u) acc = fmaf(cc[(sb + s) * Ns], xs[dy * Mx + dx], acc);
+      }
       return acc;
     };
+    float acc;
     if (sep) {
-      // Q = Qt (x) Qs: y_t = Qt_tt u_t + Qt_off (u_(t-1) + u_(t+1)), u_t = Qs x_t
-      float up = t0 > 0 ? spatial(x + int64_t(t0 - 1) * Ns + c) : 0.f;
-      float uc = spatial(x + int64_t(t0) * Ns + c);
-      for (int t = t0; t < t1; ++t) {
-        const float un = t + 1 < T ? spatial(x + int64_t(t + 1) * Ns + c) : 0.f;
-        const int64_t k = int64_t(t) * Ns + c;
-        float acc = (t == 0 || t == T - 1 ? qe : qm) * uc + qo * (up + un);
-        if (o32) acc = fmaf(o32[k], x[k], acc);
-        y[k] = acc;
-        dot = fmaf(x[k], acc, dot);
-        up = uc;
-        uc = un;
-      }
+      // Q = Qt (x) Qs: Qt_tt (Qs x_t) + Qt_off (Qs x_(t-1) + Qs x_(t+1))
+      acc = (t == 0 || t == T - 1 ? qe : qm) * block25(xt);
+      if (t > 0) acc = fmaf(qo, block25(xt - Ns), acc);
+      if (t + 1 < T) acc = fmaf(qo, block25(xt + Ns), acc);
     } else {
-      float qf[9], qb[9];
+      acc = block25(xt);
+      if (T > 1) {
+        if (t < T - 1) acc = fmaf(cc[68 * Ns], xt[0], acc);
+        if (t + 1 < T) {
 #pragma unroll
-      for (int s = 0; s < 9; ++s) {
-        qf[s] = cf[int64_t(50 + s) * Ns + c];
-        qb[s] = cf[int64_t(59 + s) * Ns + c];
-      }
-      const float cqs = cf[int64_t(68) * Ns + c];
-      for (int t = t0; t < t1; ++t) {
-        const int64_t k = int64_t(t) * Ns + c;
-        const float* xt = x + k;
-        float acc = 0.f;
-        if (t == 0 && T > 1) {
-#pragma unroll
-          for (int s = 0; s < 25; ++s)
-            if (m25 >> s & 1u) acc = fmaf(cf[int64_t(s) * Ns + c], xt[(s / 5 - 2) * Mx + (s % 5 - 2)], acc);
-        } else {
-          acc = spatial(xt);
-        }
-        if (T > 1) {
-          if (t < T - 1) acc = fmaf(cqs, xt[0], acc);
-          if (t + 1 < T) {
-#pragma unroll
-            for (int s = 0; s < 9; ++s)
-              if (m9 >> s & 1u) acc = fmaf(qf[s], xt[Ns + (s / 3 - 1) * Mx + (s % 3 - 1)], acc);
-          }
-          if (t > 0) {
-#pragma unroll
-            for (int s = 0; s < 9; ++s)
-              if (m9 >> s & 1u) acc = fmaf(qb[s], xt[-Ns + (s / 3 - 1) * Mx + (s % 3 - 1)], acc);
+          for (int s = 0; s < 9; ++s) {
+            const int dx = s % 3 - 1, dy = s / 3 - 1;
+            if ((vx >> (dx + 2)) & (vy >> (dy + 2)) & 1u) acc = fmaf(cc[(50 + s) * Ns], xt[Ns + dy * Mx + dx], acc);
           }
         }
-        if (o32) acc = fmaf(o32[k], xt[0], acc);
-        y[k] = acc;
-        dot = fmaf(xt[0], acc, dot);
+        if (t > 0) {
+#pragma unroll
+          for (int s = 0; s < 9; ++s) {
+            const int dx = s % 3 - 1, dy = s / 3 - 1;
+            if ((vx >> (dx + 2)) & (vy >> (dy + 2)) & 1u) acc = fmaf(cc[(59 + s) * Ns], xt[-Ns + dy * Mx + dx], acc);
+          }
+        }
       }
     }
+    if (o32) acc = fmaf(o32[k], xt[0], acc);
+    apv[int64_t(col) * n + k] = acc;
+    dot = xt[0] * acc;
   }
   const double bs = block_sum(dot, red);
   if (threadIdx.x == 0) part[int64_t(col) * gridDim.x + blockIdx.x] = bs;
@@ -657,7 +625,7 @@ __global__ void __launch_bounds__(256) update32c_kernel(int Ns, int T, int sep, 
     if (mode < 2) {
       float zk = rk;
       if (mode == 1) {
-        const int t = int(k / Ns), c = int(k - int64_t(t) * Ns);
+        const int t = int(k) / Ns, c = int(k) - t * Ns;  // node indices fit in 32 bits
         zk = __fdividef(rk, diag32(cf, Ns, T, sep, qe, qm, c, t) + (o32 ? o32[k] : 0.f));
       }
       zv[col * n + k] = zk;
@@ -670,119 +638,66 @@ __global__ void __launch_bounds__(256) update32c_kernel(int Ns, int T, int sep, 
   if (threadIdx.x == 0) partB[int64_t(col) * gridDim.x + blockIdx.x] = b2;
 }
 
-// Row o of G at node q (time t, cell c): the row's start and stride in the
-// weight array (compact: class row or observed row; else the per-node layout)
+// Weights of G: compact (rows per cell and time class, observed rows through
+// the bitmask and per-word ranks) or per node
 struct GWeights {
   const float* w;
   const uint32_t* mask;  // compact, with observations: observed nodes have their own rows
   const int* rank;
   int nob, Ns, T, compact;
-  __device__ __forceinline__ void row(int q, int t, int c, int64_t* base, int* stride) const {
-    if (!compact) { *base = q; *stride = Ns * T; return; }
-    if (mask) {
-      const uint32_t m = mask[q >> 5], bit = 1u << (q & 31);
-      if (m & bit) {
-        *base = int64_t(3) * kOff * Ns + rank[q >> 5] + __popc(m & (bit - 1u));
-        *stride = nob;
-        return;
-      }
-    }
-    const int k = T == 1 || t == 0 ? 0 : (t == T - 1 ? 2 : 1);
-    *base = int64_t(k) * kOff * Ns + c;
-    *stride = Ns;
-  }
 };
 
-// z = G^T G r for column blockIdx.z, one block per 32 x 8 tile of cells and
-// chunk of kGtgT time steps, and the block's partial sum of r . z.  The block
-// stages r (halo 2) and u = G r (halo 1) for three time slices in shared
-// memory, sweeping the time axis, so r is read once and u never leaves the
-// chip; the rows of G come from L1 / L2.
-constexpr int kGX = 32, kGY = 8, kGtgT = 12;
-constexpr int kRX = kGX + 4, kRY = kGY + 4, kUX = kGX + 2, kUY = kGY + 2;
-__global__ void __launch_bounds__(256) gtg32c_kernel(int Mx, int Ny, int T, GWeights gw,
-                                                     const float* __restrict__ rv, float* __restrict__ zv,
-                                                     double* __restrict__ part) {
-  __shared__ float R[3][kRY][kRX];
-  __shared__ float U[3][kUY][kUX];
-  __shared__ int UB[3][kUY][kUX];    // row start of G at the u node (-1: outside the grid)
-  __shared__ int US[3][kUY][kUX];    // its stride
+// u = G r (TRANS 0) or z = G^T u with the block's partial sum of r . z
+// (TRANS 1) for column blockIdx.y, one thread per node; the rows of G come
+// from the compact (COMPACT 1) or per-node weights through L1 / L2.  Offsets
+// fit in 32 bits (checked by the caller).
+template <int TRANS, int COMPACT>
+__global__ void __launch_bounds__(256, 4) g32n_kernel(int Mx, int Ny, int T, GWeights gw,
+                                                      const float* __restrict__ xv, float* __restrict__ outv,
+                                                      const float* __restrict__ rv, double* __restrict__ part) {
   __shared__ float red[8];
-  const int Ns = Mx * Ny;
-  const int64_t n = int64_t(Ns) * T;
-  const int col = blockIdx.z;
-  const float* r = rv + col * n;
-  float* z = zv + col * n;
-  const int ntx = (Mx + kGX - 1) / kGX;
-  const int x0 = (blockIdx.x % ntx) * kGX, y0 = (blockIdx.x / ntx) * kGY;
-  const int t0 = blockIdx.y * kGtgT, t1 = min(T, t0 + kGtgT);
-  const int tid = threadIdx.x;
-  float rz = 0.f;
-  for (int s = t0 - 2; s <= t1 + 1; ++s) {
-    // (a) r at time s, cells with halo 2
-    if (s >= 0 && s < T) {
-      float* Rs = &R[(s + 3) % 3][0][0];
-      for (int i = tid; i < kRY * kRX; i += 256) {
-        const int yy = y0 - 2 + i / kRX, xx = x0 - 2 + i % kRX;
-        Rs[i] = (xx >= 0 && xx < Mx && yy >= 0 && yy < Ny) ? r[int64_t(s) * Ns + yy * Mx + xx] : 0.f;
+  const int Ns = Mx * Ny, n = Ns * T;
+  const int col = blockIdx.y;
+  const float* x = xv + int64_t(col) * n;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  float dot = 0.f;
+  if (p < n) {
+    const int t = p / Ns, c = p - t * Ns;
+    const int y = c / Mx, xx = c - y * Mx;
+    // bit (d + 1) set: the neighbour at +-d (sign of the direction used) is inside
+    const int sg = TRANS ? -1 : 1;
+    auto bits = [](int v, int lim, int sgn) {
+      return (v - sgn >= 0 && v - sgn < lim ? 1u : 0u) | 2u | (v + sgn >= 0 && v + sgn < lim ? 4u : 0u);
+    };
+    const uint32_t bx = bits(xx, Mx, sg), by = bits(y, Ny, sg), bt = bits(t, T, sg);
+    const float* w = gw.w;
+    // the weight row of node q (time tq, cell cq) for offset o
+    auto wrow = [&](int q, int tq, int cq, int o) -> float {
+      if (!COMPACT) return w[o * n + q];
+      if (gw.mask) {
+        const uint32_t m = gw.mask[q >> 5], bit = 1u << (q & 31);
+        if (m & bit) return w[3 * kOff * Ns + o * gw.nob + gw.rank[q >> 5] + __popc(m & (bit - 1u))];
       }
-    }
-    __syncthreads();
-    // (b) u = G r at time s - 1, cells with halo 1
-    const int tu = s - 1;
-    if (tu >= t0 - 1 && tu <= t1 && tu >= 0 && tu < T) {
-      const int su = (tu + 3) % 3;
-      for (int i = tid; i < kUY * kUX; i += 256) {
-        const int ly = i / kUX, lx = i % kUX;
-        const int yy = y0 - 1 + ly, xx = x0 - 1 + lx;
-        float u = 0.f;
-        int rb = -1, rs = 0;
-        if (xx >= 0 && xx < Mx && yy >= 0 && yy < Ny) {
-          const int c = yy * Mx + xx;
-          int64_t b64;
-          gw.row(tu * Ns + c, tu, c, &b64, &rs);
-          rb = int(b64);
+      const int kc = tq == 0 ? 0 : (tq == T - 1 ? 2 : 1);
+      return w[(kc * kOff + o) * Ns + cq];
+    };
+    float acc = 0.f;
 #pragma unroll
-          for (int o = 0; o < kOff; ++o) {
-            const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
-            const int tr = tu + dt;
-            if (tr < 0 || tr >= T) continue;
-            u = fmaf(gw.w[b64 + int64_t(o) * rs], R[(tr + 3) % 3][ly + 1 + dy][lx + 1 + dx], u);
-          }
-        }
-        U[su][ly][lx] = u;
-        UB[su][ly][lx] = rb;
-        US[su][ly][lx] = rs;
-      }
+    for (int o = 0; o < kOff; ++o) {
+      const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+      if (!((bx >> (dx + 1)) & (by >> (dy + 1)) & (bt >> (dt + 1)) & 1u)) continue;
+      const int d = dt * Ns + dy * Mx + dx;
+      const int q = TRANS ? p - d : p + d;
+      const float wv = TRANS ? wrow(q, t - dt, c - dy * Mx - dx, o) : wrow(p, t, c, o);
+      acc = fmaf(wv, x[q], acc);
     }
-    __syncthreads();
-    // (c) z = G^T u at time s - 2, this block's cells
-    const int tz = s - 2;
-    if (tz >= t0 && tz < t1) {
-      const int ly = tid / kGX, lx = tid % kGX;
-      const int yy = y0 + ly, xx = x0 + lx;
-      if (xx < Mx && yy < Ny) {
-        float acc = 0.f;
-#pragma unroll
-        for (int o = 0; o < kOff; ++o) {
-          const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
-          const int tq = tz - dt;  // node q = p - o holds row o's weight for p
-          if (tq < 0 || tq >= T) continue;
-          const int sq = (tq + 3) % 3, qy = ly + 1 - dy, qx = lx + 1 - dx;
-          const int rb = UB[sq][qy][qx];
-          if (rb < 0) continue;
-          acc = fmaf(gw.w[int64_t(rb) + int64_t(o) * US[sq][qy][qx]], U[sq][qy][qx], acc);
-        }
-        const int64_t k = int64_t(tz) * Ns + yy * Mx + xx;
-        z[k] = acc;
-        rz = fmaf(R[(tz + 3) % 3][ly + 2][lx + 2], acc, rz);
-      }
-    }
-    __syncthreads();
+    outv[int64_t(col) * n + p] = acc;
+    if (TRANS) dot = rv[int64_t(col) * n + p] * acc;
   }
-  const double bs = block_sum(rz, red);
-  if (threadIdx.x == 0)
-    part[int64_t(col) * gridDim.x * gridDim.y + blockIdx.y * gridDim.x + blockIdx.x] = bs;
+  if (TRANS) {
+    const double bs = block_sum(dot, red);
+    if (threadIdx.x == 0) part[int64_t(col) * gridDim.x + blockIdx.x] = bs;
+  }
 }
 
 // Per-column scalars from block partials (one block per column, fixed order):
@@ -971,20 +886,18 @@ constexpr int kReplaceEvery = 64;
 int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const double* b, double* x, int nrhs,
               double tol, int maxit, int check_every, int* iters, double* relres) {
   const int64_t n = p->sym.n, len = n * nrhs;
-  if (len >= (int64_t(1) << 31) || nrhs > 65535) return 1;  // the stencil kernels index in 32 bits
+  // the stencil kernels index nodes, weights (27 n) and coefficients (69 Ns) in 32 bits
+  if (len >= (int64_t(1) << 31) || int64_t(p->sym.n) * kOff >= (int64_t(1) << 31) || nrhs > 65535) return 1;
   const int Mx = p->sym.Mx, Ny = p->sym.Ny, Ns = Mx * Ny, T = p->sym.T;
   cudaStream_t st = p->stream;
-  const int nch = (T + kTch - 1) / kTch;
-  const int nsp = nblk(int64_t(Ns) * nch, 128);
-  const int ntiles = ((Mx + kGX - 1) / kGX) * ((Ny + kGY - 1) / kGY), ngch = (T + kGtgT - 1) / kGtgT;
-  const int ngtg = ntiles * ngch;
-  const int na_max = std::max(nsp, std::max(int(kElemBlocks), ngtg));
+  const int nsp = nblk(n, 256);  // blocks of the per-node kernels (stencil product, G, G^T)
+  const int na_max = std::max(nsp, int(kElemBlocks));
   // FP64: true residual (row-major), block partials, per-column scalars
   const size_t need64 = size_t(len) + size_t(nrhs) * (na_max + kElemBlocks) + size_t(kDotBlocks) * nrhs +
                         size_t(8 * nrhs) + size_t(nrhs);
   double* base = scratch(p, need64);
-  // FP32 (column-major): r, z, p, Ap, x correction; coefficients; observation term; alpha, beta
-  const size_t need32 = size_t(5 * len) + size_t(kCoef32) * Ns + size_t(n) + size_t(2 * nrhs);
+  // FP32 (column-major): r, z, p, Ap, x correction, G r; coefficients; observation term; alpha, beta
+  const size_t need32 = size_t(6 * len) + size_t(kCoef32) * Ns + size_t(n) + size_t(2 * nrhs);
   float* b32 = scratch32(p, need32);
   if (!base || !b32) return 4;
   double* r64 = base;
@@ -994,8 +907,8 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
   double* sc = part64 + size_t(kDotBlocks) * nrhs;
   double *rz = sc, *pap = sc + nrhs, *rr = sc + 2 * nrhs, *bb = sc + 3 * nrhs, *rrt = sc + 4 * nrhs;
   int* done = reinterpret_cast<int*>(sc + 8 * nrhs);
-  float *r32 = b32, *z32 = r32 + len, *p32 = z32 + len, *ap32 = p32 + len, *xc32 = ap32 + len;
-  float* cf = xc32 + len;
+  float *r32 = b32, *z32 = r32 + len, *p32 = z32 + len, *ap32 = p32 + len, *xc32 = ap32 + len, *u32 = xc32 + len;
+  float* cf = u32 + len;
   float* o32 = cf + size_t(kCoef32) * Ns;
   float* alpha = o32 + n;
   float* beta = alpha + nrhs;
@@ -1019,14 +932,20 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
   coef32_kernel<<<nblk(Ns, 128), 128, 0, st>>>(q, cf);
   if (obs) obs32_kernel<<<nblk(n), 256, 0, st>>>(obs, tau, o32, n);
   const float* o = obs ? o32 : nullptr;
-  const dim3 gsp(nsp, nrhs), gel(kElemBlocks, nrhs), ggt(ntiles, ngch, nrhs);
+  const dim3 gsp(nsp, nrhs), gel(kElemBlocks, nrhs);
   // z = M r with the partial sums of r . z and r . r, after the update of r by alpha
   auto update_precond = [&]() {
     update32c_kernel<<<gel, 256, 0, st>>>(Ns, T, sep, qe, qm, mode, cf, o, xc32, r32, p32, ap32, z32, alpha, partA,
                                           partB);
-    if (mode == 2) gtg32c_kernel<<<ggt, 256, 0, st>>>(Mx, Ny, T, gw, r32, z32, partA);
+    if (mode == 2 && kind == 3) {
+      g32n_kernel<0, 1><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, r32, u32, nullptr, nullptr);
+      g32n_kernel<1, 1><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, u32, z32, r32, partA);
+    } else if (mode == 2) {
+      g32n_kernel<0, 0><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, r32, u32, nullptr, nullptr);
+      g32n_kernel<1, 0><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, u32, z32, r32, partA);
+    }
   };
-  const int na = mode == 2 ? ngtg : int(kElemBlocks);
+  const int na = mode == 2 ? nsp : int(kElemBlocks);
   // a new residual r32: z = M r, rz = r . z (p unchanged)
   auto restart = [&]() {
     cudaMemsetAsync(alpha, 0, size_t(nrhs) * sizeof(float), st);
@@ -1059,7 +978,7 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
   bool all_done = false, fresh = false;  // fresh: x holds every correction and rrt is its true residual
   for (int c = 0; c < nrhs; ++c) all_done = (c == 0 || all_done) && hd[c];
   while (it < maxit && !all_done) {
-    spmv32c_kernel<<<gsp, 128, 0, st>>>(Mx, Ny, T, sep, qe, qm, qo, cf, o, p32, ap32, partA);
+    spmv32n_kernel<<<gsp, 256, 0, st>>>(Mx, Ny, T, sep, qe, qm, qo, cf, o, p32, ap32, partA);
     scal32_kernel<<<nrhs, 256, 0, st>>>(partA, nsp, partB, 0, 0, done, rz, rr, pap, alpha, beta);
     update_precond();
     scal32_kernel<<<nrhs, 256, 0, st>>>(partA, na, partB, kElemBlocks, 1, done, rz, rr, pap, alpha, beta);
