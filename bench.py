@@ -209,8 +209,9 @@ def learned_pcg_leg(train_steps=5000, size=(400, 400, 48)):
     """Conditional-mean solve by PCG on the 400 x 400 x 48 non-stationary
     workload (7.68M nodes, seed 2, 1 % observed, right-hand side tau S^T y with
     synthetic y ~ N(0, 1)) with the learned preconditioner trained on
-    `train_steps` systems at 100 x 100 x 12 drawn from the prior, against Jacobi
-    and plain CG; tolerance 1e-6 relative residual (true residual reported)."""
+    `train_steps` systems at 100 x 100 x 12 drawn from the prior, against Jacobi,
+    incomplete-Cholesky (IC(0), natural order, level-scheduled) and plain CG;
+    tolerance 1e-6 relative residual (true residual reported)."""
     import torch
     from spdepy_gb300.precond import LearnedPreconditioner, system_maker
     from spdepy_gb300.workloads import build_model, nonstationary_advection_diffusion
@@ -238,7 +239,7 @@ def learned_pcg_leg(train_steps=5000, size=(400, 400, 48)):
            "training": {"systems": train_steps, "grid": "100x100x12", "probes_per_system": 4,
                         "seconds": round(t_train, 2), "loss_first10": float(np.mean(hist[:10])),
                         "loss_last100": float(np.mean(hist[-100:]))}}
-    for kind in ("learned", "jacobi", "none"):
+    for kind in ("learned", "jacobi", "ic0", "none"):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         wts = lp.weights(me.plan, True, tau) if kind == "learned" else None

@@ -37,6 +37,7 @@ extern "C" {
 #define SPDE_PRECOND_JACOBI 1
 #define SPDE_PRECOND_LEARNED 2
 #define SPDE_PRECOND_LEARNED_COMPACT 3 /* learned, weights from spde_precond_weights_compact */
+#define SPDE_PRECOND_IC0 4 /* incomplete Cholesky, zero fill, natural order (spde_pcg only) */
 #define SPDE_PRECOND_NPARAMS 3323
 
 typedef struct SpdePlan SpdePlan;
@@ -259,7 +260,9 @@ int spde_jacobi_smooth(SpdePlan* plan, int with_obs, double tau, double omega, i
 /* x = A^-1 b by preconditioned CG (x from 0), nrhs columns row-major, FP64
  * device; precond SPDE_PRECOND_* (w_dev: G weights for LEARNED, compact weights
  * for LEARNED_COMPACT).  The iterations run in FP32 (stencil product, vectors,
- * preconditioner); the solution is accumulated in FP64 and the residual
+ * preconditioner; IC0 factors A in FP32 on entry, level-scheduled on the
+ * lattice, with a diagonal shift raised until no pivot breaks down); the
+ * solution is accumulated in FP64 and the residual
  * replaced by the true FP64 residual b - A x whenever the recursive one has
  * fallen tenfold (and every 64 iterations).  Stops when every column's true
  * residual reaches ||b - A x|| <= tol ||b|| or after maxit iterations; *relres

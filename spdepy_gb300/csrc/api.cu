@@ -1026,8 +1026,8 @@ int spde_loglike_grad_pcg(SpdePlan* plan, double tau, const double* y, int r, co
 
 int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float* w, const double* b, double* x,
              int nrhs, double tol, int maxit, int* iters, double* relres) {
-  if (!plan || !b || !x || nrhs < 1 || maxit < 1 || !iters || !relres || precond < 0 || precond > 3 ||
-      (precond >= 2 && !w))
+  if (!plan || !b || !x || nrhs < 1 || maxit < 1 || !iters || !relres || precond < 0 || precond > 4 ||
+      ((precond == 2 || precond == 3) && !w))
     return SPDE_ERR_ARG;
   Plan& p = plan->p;
   if (precond >= 2)
@@ -1039,6 +1039,11 @@ int spde_pcg(SpdePlan* plan, int with_obs, double tau, int precond, const float*
     p.last_error = "compact preconditioner weights do not match this solve (with or without observations, or another observation set)";
     return SPDE_ERR_STATE;
   }
+  if (rc == 8) {
+    p.last_error = "IC(0) needs a spatio-temporal (not separable) plan with Mx >= 5, Ny >= 4, T >= 2";
+    return SPDE_ERR_STATE;
+  }
+  if (rc == 9) { p.last_error = "incomplete Cholesky broke down for every diagonal shift"; return SPDE_ERR_NOT_SPD; }
   if (rc == 4) { p.last_error = "scratch allocation failed"; return SPDE_ERR_NO_MEMORY; }
   if (rc == 1) { p.last_error = "n x nrhs must stay below 2^31"; return SPDE_ERR_ARG; }
   if (rc == 6) { p.last_error = "PCG did not reach the tolerance"; return SPDE_ERR_NOT_CONVERGED; }

@@ -700,6 +700,147 @@ __global__ void __launch_bounds__(256, 4) g32n_kernel(int Mx, int Ny, int T, GWe
   }
 }
 
+// ------------------------------------------------------------ IC(0)
+// Incomplete Cholesky with the pattern of A's lower triangle in the natural
+// node order (the baseline preconditioner of the PCG comparison).  The 21 lower
+// neighbours of a node, ordered by increasing node index: dt = -1 (3 x 3),
+// then dt = 0 with dy = -2, dy = -1 (dx -2..2 each) and dy = 0 (dx -2, -1).
+// Every lower neighbour of node (x, y, t) lies on an earlier level of
+// x + 3 y + 5 t, so the factorisation and the forward solve run level by
+// level (one launch per level, the backward solve in reverse).  L is FP32, 22
+// values per node: the 21 lower entries, then the diagonal.
+constexpr int kIcLow = 21, kIcRow = 22;
+struct IcTables {
+  int dx[kIcLow], dy[kIcLow], dt[kIcLow];
+  // for lower entry a: the common lower neighbours k of node i and of j = i + o_a
+  // with k < j, as (index b of k in i's row, index c of k in j's row)
+  int cstart[kIcLow + 1];
+  int cb[512], cc[512];
+};
+__constant__ IcTables c_ic;
+
+void ic_tables(IcTables* tb) {
+  int m = 0;
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) { tb->dx[m] = dx; tb->dy[m] = dy; tb->dt[m] = -1; ++m; }
+  for (int dy = -2; dy <= -1; ++dy)
+    for (int dx = -2; dx <= 2; ++dx) { tb->dx[m] = dx; tb->dy[m] = dy; tb->dt[m] = 0; ++m; }
+  for (int dx = -2; dx <= -1; ++dx) { tb->dx[m] = dx; tb->dy[m] = 0; tb->dt[m] = 0; ++m; }
+  auto find = [&](int dx, int dy, int dt) {
+    for (int i = 0; i < kIcLow; ++i)
+      if (tb->dx[i] == dx && tb->dy[i] == dy && tb->dt[i] == dt) return i;
+    return -1;
+  };
+  int e = 0;
+  for (int a = 0; a < kIcLow; ++a) {
+    tb->cstart[a] = e;
+    for (int b = 0; b < kIcLow; ++b) {
+      // k = i + o_b must precede j = i + o_a and be a lower neighbour of j: o_b - o_a lower
+      const int c = find(tb->dx[b] - tb->dx[a], tb->dy[b] - tb->dy[a], tb->dt[b] - tb->dt[a]);
+      if (c >= 0) { tb->cb[e] = b; tb->cc[e] = c; ++e; }
+    }
+  }
+  tb->cstart[kIcLow] = e;
+}
+
+// A(i, i + o) in FP32 from the coefficient copies (spatio-temporal layout)
+__device__ __forceinline__ float aval32(const float* __restrict__ cf, const float* __restrict__ o32, int Ns, int T,
+                                        int k, int c, int t, int dx, int dy, int dt) {
+  if (dt == -1) return cf[(59 + (dy + 1) * 3 + dx + 1) * Ns + c];
+  if (dt == 1) return cf[(50 + (dy + 1) * 3 + dx + 1) * Ns + c];
+  const int sb = (t == 0 && T > 1) ? 0 : 25;
+  float v = cf[(sb + (dy + 2) * 5 + dx + 2) * Ns + c];
+  if (dx == 0 && dy == 0) {
+    if (T > 1 && t < T - 1) v += cf[68 * Ns + c];
+    if (o32) v += o32[k];
+  }
+  return v;
+}
+
+// Node on level lev handled by thread e = (t, y): x = lev - 3 y - 5 t
+__device__ __forceinline__ int ic_node(int lev, int e, int Mx, int Ny, int T, int* x, int* y, int* t) {
+  if (e >= Ny * T) return -1;
+  *t = e / Ny;
+  *y = e - *t * Ny;
+  *x = lev - 3 * *y - 5 * *t;
+  if (*x < 0 || *x >= Mx) return -1;
+  return (*t * Ny + *y) * Mx + *x;
+}
+
+// One level of the factorisation of A + shift diag(A); *bad counts pivots <= 0
+__global__ void ic0_factor_kernel(int lev, int Mx, int Ny, int T, const float* __restrict__ cf,
+                                  const float* __restrict__ o32, float shift, float* __restrict__ L,
+                                  int* __restrict__ bad) {
+  int x, y, t;
+  const int i = ic_node(lev, blockIdx.x * blockDim.x + threadIdx.x, Mx, Ny, T, &x, &y, &t);
+  if (i < 0) return;
+  const int Ns = Mx * Ny, c = i - t * Ns;
+  float* Li = L + int64_t(i) * kIcRow;
+  bool in[kIcLow];
+  float dsum = 0.f;
+  for (int a = 0; a < kIcLow; ++a) {
+    const int dx = c_ic.dx[a], dy = c_ic.dy[a], dt = c_ic.dt[a];
+    in[a] = x + dx >= 0 && x + dx < Mx && y + dy >= 0 && y + dy < Ny && t + dt >= 0;
+    if (!in[a]) { Li[a] = 0.f; continue; }
+    const int j = i + dt * Ns + dy * Mx + dx;
+    const float* Lj = L + int64_t(j) * kIcRow;
+    float v = aval32(cf, o32, Ns, T, i, c, t, dx, dy, dt);
+    for (int e = c_ic.cstart[a]; e < c_ic.cstart[a + 1]; ++e) {
+      const int b = c_ic.cb[e];
+      if (in[b]) v = fmaf(-Li[b], Lj[c_ic.cc[e]], v);  // b < a: Li[b] is final
+    }
+    const float lij = v / Lj[kIcLow];
+    Li[a] = lij;
+    dsum = fmaf(lij, lij, dsum);
+  }
+  float d = aval32(cf, o32, Ns, T, i, c, t, 0, 0, 0);
+  d = d * (1.f + shift) - dsum;
+  if (!(d > 0.f)) {
+    atomicAdd(bad, 1);
+    d = 1.f;
+  }
+  Li[kIcLow] = sqrtf(d);
+}
+
+// One level of L y = r (FWD) or L^T z = y (backward), column blockIdx.y
+template <int FWD>
+__global__ void ic0_solve_kernel(int lev, int Mx, int Ny, int T, const float* __restrict__ L,
+                                 const float* __restrict__ in, float* __restrict__ out) {
+  int x, y, t;
+  const int i = ic_node(lev, blockIdx.x * blockDim.x + threadIdx.x, Mx, Ny, T, &x, &y, &t);
+  if (i < 0) return;
+  const int Ns = Mx * Ny, n = Ns * T;
+  const int64_t off = int64_t(blockIdx.y) * n;
+  float v = in[off + i];
+#pragma unroll
+  for (int a = 0; a < kIcLow; ++a) {
+    const int dx = c_ic.dx[a], dy = c_ic.dy[a], dt = c_ic.dt[a];
+    if (FWD) {
+      if (x + dx < 0 || x + dx >= Mx || y + dy < 0 || y + dy >= Ny || t + dt < 0) continue;
+      const int j = i + dt * Ns + dy * Mx + dx;
+      v = fmaf(-L[int64_t(i) * kIcRow + a], out[off + j], v);
+    } else {
+      // upper neighbour j = i - o_a, whose row holds L(j, i) at index a
+      if (x - dx < 0 || x - dx >= Mx || y - dy < 0 || y - dy >= Ny || t - dt >= T) continue;
+      const int j = i - (dt * Ns + dy * Mx + dx);
+      v = fmaf(-L[int64_t(j) * kIcRow + a], out[off + j], v);
+    }
+  }
+  out[off + i] = v / L[int64_t(i) * kIcRow + kIcLow];
+}
+
+// partial sums of a . b per block and column (column blockIdx.y)
+__global__ void __launch_bounds__(256) dot32c_kernel(const float* __restrict__ a, const float* __restrict__ b,
+                                                     int n, double* __restrict__ part) {
+  __shared__ float red[8];
+  const int64_t off = int64_t(blockIdx.y) * n;
+  float s = 0.f;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    s = fmaf(a[off + k], b[off + k], s);
+  const double bs = block_sum(s, red);
+  if (threadIdx.x == 0) part[int64_t(blockIdx.y) * gridDim.x + blockIdx.x] = bs;
+}
+
 // Per-column scalars from block partials (one block per column, fixed order):
 //   mode 0: pap = sum partA;  alpha = rz / pap (0 if done or pap <= 0)
 //   mode 1: rzn = sum partA, rr = sum partB;  beta = rzn / rz, rz = rzn
@@ -897,7 +1038,8 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
                         size_t(8 * nrhs) + size_t(nrhs);
   double* base = scratch(p, need64);
   // FP32 (column-major): r, z, p, Ap, x correction, G r; coefficients; observation term; alpha, beta
-  const size_t need32 = size_t(6 * len) + size_t(kCoef32) * Ns + size_t(n) + size_t(2 * nrhs);
+  const size_t need32 = size_t(6 * len) + size_t(kCoef32) * Ns + size_t(n) + size_t(2 * nrhs) +
+                        (kind == 4 ? size_t(kIcRow) * n : 0);
   float* b32 = scratch32(p, need32);
   if (!base || !b32) return 4;
   double* r64 = base;
@@ -912,11 +1054,14 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
   float* o32 = cf + size_t(kCoef32) * Ns;
   float* alpha = o32 + n;
   float* beta = alpha + nrhs;
+  float* Lic = beta + nrhs;  // IC(0) factor (kind 4)
   const QStencil q = p->qstencil();
   const double* obs = with_obs ? p->d_obs_cnt : nullptr;
   const int sep = q.sep;
   const float qe = float(q.qt_end), qm = float(q.qt_mid), qo = float(q.qt_off);
-  const int mode = kind == 0 ? 0 : (kind == 1 ? 1 : 2);
+  const int mode = kind == 0 ? 0 : (kind == 1 ? 1 : 2);  // 2: z from a separate preconditioner pass
+  // IC(0) of the spatio-temporal stencil; its lower-neighbour order needs Mx >= 5, Ny >= 4
+  if (kind == 4 && (q.sep || T < 2 || Mx < 5 || Ny < 4)) return 8;
   if (kind == 3) {
     // compact weights hold observed rows for the observation set they were computed with
     int head[kCompactHeader] = {0, 0, 0, 0};
@@ -933,6 +1078,30 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
   if (obs) obs32_kernel<<<nblk(n), 256, 0, st>>>(obs, tau, o32, n);
   const float* o = obs ? o32 : nullptr;
   const dim3 gsp(nsp, nrhs), gel(kElemBlocks, nrhs);
+  const int nlev = (Mx - 1) + 3 * (Ny - 1) + 5 * (T - 1) + 1;
+  const dim3 glev(nblk(int64_t(Ny) * T, 128), nrhs);
+  if (kind == 4) {
+    // IC(0) of A + shift diag(A), the shift raised until no pivot breaks down
+    static IcTables tables;
+    static const bool tables_ready = (ic_tables(&tables), true);
+    (void)tables_ready;
+    if (cudaMemcpyToSymbolAsync(c_ic, &tables, sizeof(IcTables), 0, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return 2;
+    int* bad = reinterpret_cast<int*>(alpha);  // alpha is set before its first use
+    const float shifts[] = {0.f, 1e-3f, 1e-2f, 1e-1f, 1.f};
+    bool ok = false;
+    for (float sh : shifts) {
+      cudaMemsetAsync(bad, 0, sizeof(int), st);
+      for (int lev = 0; lev < nlev; ++lev)
+        ic0_factor_kernel<<<nblk(int64_t(Ny) * T, 128), 128, 0, st>>>(lev, Mx, Ny, T, cf, o, sh, Lic, bad);
+      int hb = 0;
+      if (cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return 2;
+      if (hb == 0) { ok = true; break; }
+    }
+    if (!ok) return 9;
+  }
   // z = M r with the partial sums of r . z and r . r, after the update of r by alpha
   auto update_precond = [&]() {
     update32c_kernel<<<gel, 256, 0, st>>>(Ns, T, sep, qe, qm, mode, cf, o, xc32, r32, p32, ap32, z32, alpha, partA,
@@ -940,6 +1109,12 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
     if (mode == 2 && kind == 3) {
       g32n_kernel<0, 1><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, r32, u32, nullptr, nullptr);
       g32n_kernel<1, 1><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, u32, z32, r32, partA);
+    } else if (kind == 4) {
+      for (int lev = 0; lev < nlev; ++lev)
+        ic0_solve_kernel<1><<<glev, 128, 0, st>>>(lev, Mx, Ny, T, Lic, r32, u32);
+      for (int lev = nlev - 1; lev >= 0; --lev)
+        ic0_solve_kernel<0><<<glev, 128, 0, st>>>(lev, Mx, Ny, T, Lic, u32, z32);
+      dot32c_kernel<<<gsp, 256, 0, st>>>(r32, z32, int(n), partA);
     } else if (mode == 2) {
       g32n_kernel<0, 0><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, r32, u32, nullptr, nullptr);
       g32n_kernel<1, 0><<<gsp, 256, 0, st>>>(Mx, Ny, T, gw, u32, z32, r32, partA);

@@ -271,13 +271,14 @@ class GPUPlan:
         return z
 
     def pcg(self, b, with_obs=False, tau=0.0, precond="jacobi", w=None, tol=1e-8, maxit=20000, check=True):
-        """x = A^-1 b by preconditioned CG; precond "none", "jacobi" or "learned" (w: per-node
-        weights, or the CompactWeights of precond_weights_compact)."""
+        """x = A^-1 b by preconditioned CG; precond "none", "jacobi", "ic0" (incomplete
+        Cholesky) or "learned" (w: per-node weights, or the CompactWeights of
+        precond_weights_compact)."""
         torch = _torch()
         b = b.to(device="cuda", dtype=torch.float64).contiguous()
         nrhs = 1 if b.dim() == 1 else b.shape[1]
         x = torch.empty_like(b)
-        kind = {"none": 0, "jacobi": 1, "learned": 2}[precond]
+        kind = {"none": 0, "jacobi": 1, "learned": 2, "ic0": 4}[precond]
         if kind == 2 and isinstance(w, CompactWeights):
             kind, w = 3, w.data
         it, rel = ctypes.c_int(), ctypes.c_double()
