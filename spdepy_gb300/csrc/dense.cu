@@ -964,16 +964,30 @@ __global__ void __launch_bounds__(256) extend_add_kernel(const ExtendTask* __res
   const T* U = Uc + c.u_off;
   T* P = L + p.p_off;
   T* Upar = Up + p.u_off;
-  for (int i = tk.r0; i < tk.r1; ++i) {
-    const int pi = rm[i];
-    const T* urow = U + int64_t(i) * c.ldu;
-    for (int j = threadIdx.x; j <= i; j += blockDim.x) {
-      const int pj = rm[j];
-      const T v = urow[j];
-      if (pj < p.ns) P[int64_t(pi) * p.ld + pj] += v;
-      else Upar[int64_t(pi - p.ns) * p.ldu + (pj - p.ns)] += v;
-    }
+  // one warp per row of the task (up to 8), four independent elements in flight
+  // per lane; row i adds its lower part j <= i into the parent's row rm[i]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = tk.r0 + warp;
+  if (i >= tk.r1) return;
+  const int pi = rm[i];
+  const T* urow = U + int64_t(i) * c.ldu;
+  T* prow = P + int64_t(pi) * p.ld;
+  // pj >= ns implies pi >= ns (rm increases and j <= i): the parent's update block
+  T* urw = pi >= p.ns ? Upar + int64_t(pi - p.ns) * p.ldu : nullptr;
+  auto add = [&](int pj, T v) {
+    if (pj < p.ns) prow[pj] += v;
+    else urw[pj - p.ns] += v;
+  };
+  int j = lane;
+  for (; j + 96 <= i; j += 128) {
+    const int q0 = rm[j], q1 = rm[j + 32], q2 = rm[j + 64], q3 = rm[j + 96];
+    const T v0 = urow[j], v1 = urow[j + 32], v2 = urow[j + 64], v3 = urow[j + 96];
+    add(q0, v0);
+    add(q1, v1);
+    add(q2, v2);
+    add(q3, v3);
   }
+  for (; j <= i; j += 32) add(rm[j], urow[j]);
 }
 
 template <typename T>

@@ -726,11 +726,23 @@ __global__ void zgather_kernel(const RowTask* __restrict__ tasks, const DevFront
   const DevFront f = F[tk.front];
   const DevFront p = F[f.parent];
   const int* rm = rmap + f.b_off;
-  for (int a = tk.r0; a < tk.r1; ++a) {
-    const T* src = Zp + p.z_off + int64_t(rm[a]) * p.ldz;
-    T* dst = Zc + f.z_off + int64_t(f.ns + a) * f.ldz + f.ns;
-    for (int bcol = threadIdx.x; bcol < f.nb; bcol += blockDim.x) dst[bcol] = src[rm[bcol]];
+  // one warp per row (up to 8 rows per task), four independent elements in
+  // flight per lane: the gather is latency-bound otherwise
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int a = tk.r0 + warp;
+  if (a >= tk.r1) return;
+  const T* src = Zp + p.z_off + int64_t(rm[a]) * p.ldz;
+  T* dst = Zc + f.z_off + int64_t(f.ns + a) * f.ldz + f.ns;
+  int bcol = lane;
+  for (; bcol + 96 < f.nb; bcol += 128) {
+    const int c0 = rm[bcol], c1 = rm[bcol + 32], c2 = rm[bcol + 64], c3 = rm[bcol + 96];
+    const T v0 = src[c0], v1 = src[c1], v2 = src[c2], v3 = src[c3];
+    dst[bcol] = v0;
+    dst[bcol + 32] = v1;
+    dst[bcol + 64] = v2;
+    dst[bcol + 96] = v3;
   }
+  for (; bcol < f.nb; bcol += 32) dst[bcol] = src[rm[bcol]];
 }
 
 template <typename T>
