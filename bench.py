@@ -35,9 +35,9 @@ METRIC = "logL+grad evals/s & samples/s, 200x200x24 SPDE: mixed+learned vs FP64 
 
 
 # DRAM bytes per algorithmic flop of the tensor-core product, from the ncu
-# captures of its two largest launches at 100 x 100 x 24 (an inverse-block
-# product, 4.430e11 flops, and a Schur update, 2.270e11 flops): 2.200e9 bytes.
-TC_DRAM_BYTES_PER_FLOP = 2.200e9 / 6.700e11
+# capture of the largest cluster-pair launch at 100 x 100 x 24 (an inverse-block
+# product of 4.430e11 flops: 1.294e9 bytes read, 0.156e9 written).
+TC_DRAM_BYTES_PER_FLOP = 1.450e9 / 4.430e11
 
 
 def _tf32_tflops(torch, n=8192, reps=10):
@@ -583,12 +583,13 @@ def main():
                 "d2h_bytes_per_step": int(canon.size) * 8 + 8},
         "samples_per_s": samples_per_s,
         "gpu_launches": int(launches),
-        "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel (3xTF32 tiled product: factor and inverse updates)",
+        "roofline": {"bound": "tensor", "kernel": "tc_pair_kernel + tc_gemm_kernel (3xTF32 tiled products: factor and "
+                                                  "inverse updates; cluster pairs on 256x256 tiles, single CTAs below)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": f"bf16 dense, sustained, {peak_src}",
                      "traffic": TC_DRAM_BYTES_PER_FLOP * tc_flops_per_launch,
-                     "traffic_source": "ncu dram bytes per flop of two captured launches (100x100x24), "
-                                       "scaled by this run's flops per launch",
+                     "traffic_source": "ncu dram bytes per flop of the largest captured pair launch "
+                                       "(100x100x24), scaled by this run's flops per launch",
                      "launches_per_step": float(pct[9] / args.steps),
                      "note": "CUDA events around each tensor-core launch in the timed region, while the Q and "
                              "Q + tau S^T S pipelines run concurrently on two streams; the per-class split below "

@@ -873,8 +873,9 @@ void prof_collect(Plan* p) {
 
 // Optional launch log of the tensor-core tiled product: with SPDE_LAUNCH_LOG set
 // to a file name, one line per launch (process-wide launch number, call site,
-// tiles, algorithmic flops), so that a profiler capture of the n-th launch can be
-// matched with the work it did.  Host-side bookkeeping only.
+// tasks, algorithmic flops, path: 1 single-CTA tiles, 4 cluster pairs), so that
+// a profiler capture of the n-th launch can be matched with the work it did.
+// Host-side bookkeeping only.
 static void tc_launch_log(const Op& o) {
   static std::mutex mu;
   static FILE* fh = nullptr;
@@ -885,10 +886,10 @@ static void tc_launch_log(const Op& o) {
     opened = true;
     const char* path = std::getenv("SPDE_LAUNCH_LOG");
     if (path && *path) fh = std::fopen(path, "w");
-    if (fh) std::fprintf(fh, "launch site tiles flops\n");
+    if (fh) std::fprintf(fh, "launch site tiles flops path\n");
   }
   if (fh) {
-    std::fprintf(fh, "%lld %d %d %.0f\n", static_cast<long long>(seq), o.site, o.count, o.flops);
+    std::fprintf(fh, "%lld %d %d %.0f %d\n", static_cast<long long>(seq), o.site, o.count, o.flops, o.tc);
     std::fflush(fh);
   }
   ++seq;
