@@ -207,7 +207,38 @@ struct SpdePlan {
   // and the observations of `p` (read only) and is built on first use.
   std::unique_ptr<Plan> twin;
   int pipelines = 2;
+  // phase streams of the two pipelines: [pipeline][0 factor / solve, 1 inverse],
+  // and the events that order a pipeline's phases across them
+  cudaStream_t phase[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  cudaEvent_t phase_ev[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
 };
+
+// Moves a plan's subsequent work to stream `to`, after everything enqueued so far.
+static void move_to(Plan* p, cudaStream_t to, cudaEvent_t ev) {
+  if (to == p->stream) return;
+  cudaEventRecord(ev, p->stream);
+  cudaStreamWaitEvent(to, ev, 0);
+  p->stream = to;
+}
+
+// Creates the phase streams: the factorisations and the solve, chains of
+// latency-bound launches, at the greatest priority; the selected inversions,
+// long runs of large tensor-core products, at the least, so that they fill the
+// SMs the chains leave idle without delaying them.
+static int ensure_phase_streams(SpdePlan* plan) {
+  if (plan->phase[0][0]) return SPDE_OK;
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  for (int q = 0; q < 2; ++q)
+    for (int k = 0; k < 2; ++k)
+      if (cudaStreamCreateWithPriority(&plan->phase[q][k], cudaStreamNonBlocking, k == 0 ? greatest : least) !=
+          cudaSuccess)
+        return SPDE_ERR_CUDA;
+  for (int q = 0; q < 2; ++q)
+    for (int k = 0; k < 3; ++k)
+      if (cudaEventCreateWithFlags(&plan->phase_ev[q][k], cudaEventDisableTiming) != cudaSuccess) return SPDE_ERR_CUDA;
+  return SPDE_OK;
+}
 
 extern "C" {
 
@@ -388,6 +419,12 @@ int spde_plan_destroy(SpdePlan* plan) {
   destroy_twin(plan);
   Plan& p = plan->p;
   cudaStreamSynchronize(p.stream);
+  for (auto& row : plan->phase)
+    for (cudaStream_t& q : row)
+      if (q) { cudaStreamSynchronize(q); cudaStreamDestroy(q); }
+  for (auto& row : plan->phase_ev)
+    for (cudaEvent_t& e : row)
+      if (e) cudaEventDestroy(e);
   void* ptrs[] = {p.d_fronts, p.d_perm, p.d_iperm, p.d_front_of, p.d_blist, p.d_rmap, p.d_amap, p.d_L, p.d_dinv,
                   p.d_pool[0], p.d_pool[1], p.d_logpiv, p.d_err, p.d_scalar, p.d_bs, p.d_bsH, p.d_bsA, p.d_ww,
                   p.d_theta, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.d_obs_cnt,
@@ -796,7 +833,13 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
   double ldq = 0.0, ldqc = 0.0, res = 0.0, res_c = 0.0;
   int rc_c = 0;
   PhaseLog plog(st);
+  // with two pipelines, each runs its phases on the plan's phase streams and
+  // returns to its own stream at the end
+  bool phased = qc != &p;
+  if (phased && (rc = ensure_phase_streams(plan))) return rc;
+  cudaStream_t qc_home = qc->stream;
   auto run_qc = [&]() {
+    if (phased) move_to(qc, plan->phase[1][0], plan->phase_ev[1][0]);
     if ((rc_c = plan_factor(qc, 1, tau))) return;
     plog.mark("qc_factor", qc->stream);
     ldqc = qc->logdet;
@@ -806,6 +849,7 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
     if ((rc_c = plan_solve(qc, S.b.p, S.mu.p, r, iters, tol, &res_c))) return;
     plog.mark("qc_solve", qc->stream);
     if (hutch && (rc_c = plan_solve(qc, V, S.trc.p, nh1, iters, tol, &res_c))) return;
+    if (phased) move_to(qc, plan->phase[1][1], plan->phase_ev[1][1]);
     if (exact && (rc_c = plan_selinv(qc, S.zqc.p))) return;
     plog.mark("qc_inverse", qc->stream);
   };
@@ -815,17 +859,26 @@ int spde_loglike(SpdePlan* plan, const double* theta, int ntheta, const double* 
       worker = std::thread(run_qc);
     } catch (...) {
       qc = &p;  // no thread available: both on this plan, one after the other
+      phased = false;
     }
   }
   // Q: log-determinant, then its inverse on the pattern (or Hutchinson solves)
+  if (phased) move_to(&p, plan->phase[0][0], plan->phase_ev[0][0]);
   rc = plan_factor(&p, 0, 0.0);
-  plog.mark("q_factor", st);
+  plog.mark("q_factor", p.stream);
   if (!rc) ldq = p.logdet;
+  if (phased) move_to(&p, plan->phase[0][1], plan->phase_ev[0][1]);
   if (!rc && exact) rc = plan_selinv(&p, S.zq.p);
-  plog.mark("q_inverse", st);
+  plog.mark("q_inverse", p.stream);
   if (!rc && hutch) rc = plan_solve(&p, V, S.trq.p, nh1, iters, tol, &res);
   if (qc != &p) worker.join();
   else if (!rc) run_qc();
+  if (phased) {
+    // back to the caller's stream, after both pipelines' work
+    move_to(qc, qc_home, plan->phase_ev[1][2]);
+    cudaStreamWaitEvent(st, plan->phase_ev[1][2], 0);
+    move_to(&p, st, plan->phase_ev[0][2]);
+  }
   if (rc) return rc;
   if (rc_c) {
     if (qc != &p) p.last_error = qc->last_error;

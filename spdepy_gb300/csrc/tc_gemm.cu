@@ -401,12 +401,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const GemmTask* __
 // kernel.  The converters zero every k >= K of the last chunk, so a box may
 // read past the task's K range.
 //
-// Only the even CTA issues MMAs.  Both CTAs' converter warps arrive on its
-// ready[s] (16 arrivals: 8 warps x 2 CTAs); its tcgen05.commit arrives on
+// Two groups of eight converter warps take alternate chunks, so that two
+// chunks are split at a time (one group's split latency no longer bounds the
+// tensor core); both groups then share the epilogue, 64 accumulator columns per
+// warp.  Only the even CTA issues MMAs.  The converter warps that took chunk t
+// in both CTAs arrive on its ready[s] (16 arrivals: 8 warps x 2 CTAs); its
+// tcgen05.commit arrives on
 // consumed[s] and, after the last chunk, on done in both CTAs.  Neither CTA
 // frees its tensor memory or exits before the pair's MMAs are done (a wait on
 // done, then a cluster barrier), also after a failed (timed-out) wait.
 constexpr int kPairASlot0 = 256;  // TMEM: accumulator columns 0-255, A slot s at 256 + 64 s
+constexpr int kPairGroups = 2;     // converter groups of the pair kernel (group g takes chunks t = g mod 2)
+constexpr int kPairThreads = kPairGroups * kConv + kLoad + 32;  // warps 0-15 converters, 16-19 loaders, 20 MMA
+constexpr int kPairEpiCols = 256 / (kPairGroups * kConv / 128);  // accumulator columns per epilogue warp
 constexpr uint32_t kIdescPair = (1u << 4) | (2u << 7) | (2u << 10) | ((256u >> 3) << 17) | ((256u >> 4) << 24);
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -501,7 +508,7 @@ __device__ __forceinline__ void split_b_masked(uint8_t* raw, uint8_t* lo, int ti
 }
 
 template <int MODE>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     tc_pair_kernel(const GemmTask* __restrict__ tasks, const CUtensorMap* __restrict__ maps, const float* Ab,
                    const float* Bb, float* Cb, unsigned long long wait_ns) {
   extern __shared__ uint8_t smem_raw[];
@@ -560,10 +567,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
     return true;
   };
 
-  if (warp < kConv / 32) {
-    // ---------------- converters, then the epilogue
+  if (warp < kPairGroups * kConv / 32) {
+    // ---------------- converters (two groups on alternate chunks), then the epilogue
     const uint32_t lane_base = uint32_t((warp & 3) * 32) << 16;
-    for (int t = 0; t < nk; ++t) {
+    const int g = warp / (kConv / 32), ct = tid - g * kConv;
+    for (int t = g; t < nk; t += kPairGroups) {
       const int s = t % kStages;
       if (!wait(&full[s], uint32_t((t / kStages) & 1), true, wait_ns)) break;
       if ((atma || btma) && !wait(&tfull[s], uint32_t((t / kStages) & 1), true, wait_ns)) break;
@@ -571,11 +579,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
       const int kvalid = tk.k - t * kTK;
       const uint32_t slot = tmem + lane_base + uint32_t(kPairASlot0 + s * kASlotCols);
       if (kvalid >= kTK) {
-        a_to_tmem(st, tid & 127, tid >> 7, slot);
-        split_b(st + kPlane, st + 2 * kPlane, tid);
+        a_to_tmem(st, ct & 127, ct >> 7, slot);
+        split_b(st + kPlane, st + 2 * kPlane, ct);
       } else {
-        a_to_tmem_masked(st, tid & 127, tid >> 7, slot, kvalid);
-        split_b_masked(st + kPlane, st + 2 * kPlane, tid, kvalid);
+        a_to_tmem_masked(st, ct & 127, ct >> 7, slot, kvalid);
+        split_b_masked(st + kPlane, st + 2 * kPlane, ct, kvalid);
       }
       asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -586,12 +594,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
     const bool fin = nk > 0 && wait(&done, 0u, true, wait_ns);
     if (fin) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      // warp w reads lanes 32 (w % 4) .. and accumulator columns 128 (w / 4) ..
+      // warp w reads lanes 32 (w % 4) .. and accumulator columns kPairEpiCols (w / 4) ..
       const int row = (warp & 3) * 32 + lane;
       const int grow = row0 + row;
 #pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        const int col0 = (warp >> 2) * 128 + c * 32;
+      for (int c = 0; c < kPairEpiCols / 32; ++c) {
+        const int col0 = (warp >> 2) * kPairEpiCols + c * 32;
         uint32_t r[32];
         const uint32_t ta = tmem + lane_base + uint32_t(col0);
         asm volatile(
@@ -635,9 +643,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
         }
       }
     }
-  } else if (warp < (kConv + kLoad) / 32) {
+  } else if (warp < (kPairGroups * kConv + kLoad) / 32) {
     // ---------------- loaders: TMA boxes (one elected thread) and / or cp.async
-    const int ltid = tid - kConv;
+    const int ltid = tid - kPairGroups * kConv;
     int issued = 0;  // chunks whose TMA boxes this thread (ltid 0) issued
     for (int t = 0; t < nk; ++t) {
       const int s = t % kStages;
@@ -715,7 +723,7 @@ void launch_pair(const GemmTask* t, int n, const CUtensorMap* maps, const float*
     return true;
   }();
   (void)attr;
-  tc_pair_kernel<MODE><<<2 * n, kThreads, kSmem, st>>>(t, maps, A, B, C, wait_ns);
+  tc_pair_kernel<MODE><<<2 * n, kPairThreads, kSmem, st>>>(t, maps, A, B, C, wait_ns);
 }
 
 template <int MODE, int AL, int BL>
