@@ -301,6 +301,8 @@ static void release_numeric(Plan& p) {
                   p.d_pool[0], p.d_pool[1], p.d_logpiv, p.d_err, p.d_scalar, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0],
                   p.d_G[1], p.d_r, p.d_x64, p.d_b64, p.d_part, p.d_sx, p.d_pc};
   for (void* q : ptrs) cudaFree(q);
+  cudaFreeHost(p.h_pin);
+  p.h_pin = nullptr;
   for (cudaEvent_t e : p.ev_pool) cudaEventDestroy(e);
   p.ev_pool.clear();
   p.sched_factor.release();
@@ -431,6 +433,8 @@ int spde_plan_destroy(SpdePlan* plan) {
                   p.d_obs_idx, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0], p.d_G[1], p.d_r, p.d_x64, p.d_b64,
                   p.d_obs_mask, p.d_obs_rank, p.d_obs_nodes, p.d_pc32};
   for (void* q : ptrs) cudaFree(q);
+  cudaFreeHost(p.h_pin);
+  p.h_pin = nullptr;
   cudaFree(p.d_part);
   cudaFree(p.d_sx);
   cudaFree(p.d_pc);

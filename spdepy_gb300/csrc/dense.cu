@@ -951,54 +951,73 @@ template void launch_potrf<float>(const DiagTask*, int, float*, float*, double*,
 // Adds the lower triangle of a child's update block into its parent's front:
 // columns inside the parent separator go to the parent panel P, the rest to the
 // parent's own update block U.  One launch per child rank, so no two blocks of
-// a launch touch the same parent entry.
+// a launch touch the same parent entry.  A task is a range of the child's rows
+// [r0, r1) (more rows when they are short); the row map entries rm[0 .. r1) that
+// its rows use as column targets are staged in shared memory first (up to
+// kExtendSmemRows of them, else read from global memory), so that the
+// read-modify-write of each element waits on one global load, not two.
+constexpr int kExtendSmemRows = 12288;  // 48 KB of row map per block
+
 template <typename T>
 __global__ void __launch_bounds__(256) extend_add_kernel(const ExtendTask* __restrict__ tasks,
                                                          const DevFront* __restrict__ fronts,
                                                          const int* __restrict__ rmap, const T* __restrict__ Uc,
                                                          T* __restrict__ L, T* __restrict__ Up) {
+  extern __shared__ int srm[];
   const ExtendTask tk = tasks[blockIdx.x];
   const DevFront c = fronts[tk.child];
   const DevFront p = fronts[c.parent];
   const int* rm = rmap + c.b_off;
+  const bool staged = tk.r1 <= kExtendSmemRows;
+  if (staged)
+    for (int e = threadIdx.x; e < tk.r1; e += blockDim.x) srm[e] = rm[e];
+  __syncthreads();
+  const int* cm = staged ? srm : rm;
   const T* U = Uc + c.u_off;
   T* P = L + p.p_off;
   T* Upar = Up + p.u_off;
-  // one warp per row of the task (up to 8), four independent elements in flight
-  // per lane; row i adds its lower part j <= i into the parent's row rm[i]
+  // one warp per row (rows r0 + warp, r0 + warp + 8, ...), eight elements in
+  // flight per lane; row i adds its lower part j <= i into the parent's row rm[i]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = tk.r0 + warp;
-  if (i >= tk.r1) return;
-  const int pi = rm[i];
-  const T* urow = U + int64_t(i) * c.ldu;
-  T* prow = P + int64_t(pi) * p.ld;
-  // pj >= ns implies pi >= ns (rm increases and j <= i): the parent's update block
-  T* urw = pi >= p.ns ? Upar + int64_t(pi - p.ns) * p.ldu : nullptr;
-  auto add = [&](int pj, T v) {
-    if (pj < p.ns) prow[pj] += v;
-    else urw[pj - p.ns] += v;
-  };
-  int j = lane;
-  for (; j + 96 <= i; j += 128) {
-    const int q0 = rm[j], q1 = rm[j + 32], q2 = rm[j + 64], q3 = rm[j + 96];
-    const T v0 = urow[j], v1 = urow[j + 32], v2 = urow[j + 64], v3 = urow[j + 96];
-    add(q0, v0);
-    add(q1, v1);
-    add(q2, v2);
-    add(q3, v3);
+  for (int i = tk.r0 + warp; i < tk.r1; i += 8) {
+    const int pi = cm[i];
+    const T* urow = U + int64_t(i) * c.ldu;
+    T* prow = P + int64_t(pi) * p.ld;
+    // pj >= ns implies pi >= ns (rm increases and j <= i): the parent's update block
+    T* urw = pi >= p.ns ? Upar + int64_t(pi - p.ns) * p.ldu : nullptr;
+    auto target = [&](int pj) -> T* { return pj < p.ns ? prow + pj : urw + (pj - p.ns); };
+    int j = lane;
+    for (; j + 224 <= i; j += 256) {
+      T v[8];
+      T* d[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        v[u] = urow[j + 32 * u];
+        d[u] = target(cm[j + 32 * u]);
+      }
+      T o[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) o[u] = *d[u];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) *d[u] = o[u] + v[u];
+    }
+    for (; j <= i; j += 32) {
+      T* d = target(cm[j]);
+      *d += urow[j];
+    }
   }
-  for (; j <= i; j += 32) add(rm[j], urow[j]);
 }
 
 template <typename T>
 void launch_extend_add(const ExtendTask* tasks, int ntasks, const DevFront* fronts, const int* rmap, const T* U_child,
-                       T* L, T* U_parent, cudaStream_t st) {
+                       T* L, T* U_parent, int max_r1, cudaStream_t st) {
   if (ntasks <= 0) return;
-  extend_add_kernel<T><<<ntasks, 256, 0, st>>>(tasks, fronts, rmap, U_child, L, U_parent);
+  const size_t smem = size_t(max_r1 <= kExtendSmemRows ? max_r1 : 0) * sizeof(int);
+  extend_add_kernel<T><<<ntasks, 256, smem, st>>>(tasks, fronts, rmap, U_child, L, U_parent);
 }
 template void launch_extend_add<double>(const ExtendTask*, int, const DevFront*, const int*, const double*, double*,
-                                        double*, cudaStream_t);
+                                        double*, int, cudaStream_t);
 template void launch_extend_add<float>(const ExtendTask*, int, const DevFront*, const int*, const float*, float*,
-                                       float*, cudaStream_t);
+                                       float*, int, cudaStream_t);
 
 }  // namespace spde

@@ -265,8 +265,15 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
       for (int f : fr) {
         int c = F[f].child[rank];
         if (c < 0 || F[c].nb == 0) continue;
-        const int chunk = 8;
-        for (int r0 = 0; r0 < F[c].nb; r0 += chunk) sc.ext.push_back({c, r0, std::min(F[c].nb, r0 + chunk)});
+        // about 16k elements per block (row r holds r + 1): 8 rows of the long
+        // rows, up to 128 of the short ones
+        for (int r0 = 0; r0 < F[c].nb;) {
+          const int rows = std::max(8, std::min(128, (16384 / (r0 + 1)) & ~7));
+          const int r1 = std::min(F[c].nb, r0 + rows);
+          sc.ext.push_back({c, r0, r1});
+          o.nmax = std::max(o.nmax, r1);
+          r0 = r1;
+        }
       }
       b.end();
     }
@@ -938,7 +945,7 @@ struct Exec {
         case OP_MEMSET: cudaMemsetAsync(buf(o.cbuf), 0, size_t(o.elems) * sizeof(T), st); break;
         case OP_EXTEND:
           launch_extend_add<T>(s.d_ext + o.off, o.count, p->d_fronts, p->d_rmap, buf(o.abuf), buf(B_L), buf(o.cbuf),
-                               st);
+                               o.nmax, st);
           break;
         case OP_DIAG:
           launch_potrf<T>(s.d_diag + o.off, o.count, buf(B_L), buf(B_DINV), p->d_logpiv + o.off, p->d_err, st);
@@ -1107,6 +1114,7 @@ int plan_build(Plan* p) {
   CUDA_TRY(cudaMalloc(&p->d_err, sizeof(int)));
   CUDA_TRY(cudaMalloc(&p->d_scalar, 64 * sizeof(double)));
   CUDA_TRY(cudaMalloc(&p->d_part, 1024 * sizeof(double)));
+  CUDA_TRY(cudaMallocHost(&p->h_pin, 2048 * sizeof(double)));
   return 0;
 }
 
@@ -1115,19 +1123,18 @@ static int factor_t(Plan* p, int with_obs, double tau) {
   const Symbolic& S = p->sym;
   cudaStream_t st = p->stream;
   CUDA_TRY(cudaMemsetAsync(p->d_L, 0, size_t(S.l_size) * sizeof(T), st));
-  int m1 = -1;
-  CUDA_TRY(cudaMemcpyAsync(p->d_err, &m1, sizeof(int), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(p->d_err, 0xFF, sizeof(int), st));  // -1: no failed pivot
   launch_scatter<T>(p->qstencil(), S.nslots, p->d_amap, p->d_perm, p->d_front_of, p->d_fronts,
                     with_obs ? p->d_obs_cnt : nullptr, tau, static_cast<T*>(p->d_L), st);
   Exec<T>{p, p->sched_factor, 0, nullptr}.run();
   sum_kernel<<<1, 256, 0, st>>>(p->d_logpiv, int64_t(p->sched_factor.diag.size()), p->d_scalar);
-  double sum = 0.0;
-  int err = -1;
-  CUDA_TRY(cudaMemcpyAsync(&sum, p->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaMemcpyAsync(&err, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(p->h_pin + 1024, p->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(p->pin_int(), p->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   CUDA_TRY(cudaGetLastError());
-  if (tc_gemm_take_error(p->stream)) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
+  const double sum = p->h_pin[1024];
+  const int err = p->pin_int()[0];
+  if (tc_gemm_take_error(p->stream, p->pin_int() + 1)) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
   if (err >= 0) {
     char buf[128];
     std::snprintf(buf, sizeof(buf), "matrix is not positive definite (front %d)", err);
@@ -1205,40 +1212,43 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
   tri_solve<T>(p, nrhs);
   launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 0, st);
   p->launches_total += 2;
-  double rel = -1.0;
   const int nblk = 512;
-  std::vector<double> part(2 * nblk);
-  for (int it = 0; it < iters; ++it) {
+  // relative residual ||b - A x|| / ||b|| of the current x (partial sums read
+  // through the plan's page-locked buffer)
+  auto residual = [&]() -> double {
     launch_spmv(p->qstencil(), obs, tau, x, p->d_r, nrhs, st);
     resid_kernel<<<nblk, 256, 0, st>>>(b, p->d_r, ne, p->d_part);
     p->launches_total += 2;
-    CUDA_TRY(cudaMemcpyAsync(part.data(), p->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
+    if (cudaMemcpyAsync(p->h_pin, p->d_part, 2 * nblk * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return -1.0;
     double r2 = 0.0, b2 = 0.0;
-    for (int k = 0; k < nblk; ++k) { r2 += part[2 * k]; b2 += part[2 * k + 1]; }
-    rel = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    for (int k = 0; k < nblk; ++k) { r2 += p->h_pin[2 * k]; b2 += p->h_pin[2 * k + 1]; }
+    return b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+  };
+  double rel = -1.0;
+  bool fresh = false;  // rel belongs to the current x
+  for (int it = 0; it < iters; ++it) {
+    rel = residual();
+    if (rel < 0) { p->last_error = "residual read-back failed"; return 2; }
+    fresh = true;
     if (rel <= tol) break;
     p->launches_total += 2;
     launch_to_new<T>(p->d_r, p->d_perm, n, nrhs, static_cast<T*>(p->d_X), st);
     tri_solve<T>(p, nrhs);
     launch_from_new<T>(static_cast<const T*>(p->d_X), p->d_perm, n, nrhs, x, 1, st);
+    fresh = false;
   }
   if (resid) {
-    if (rel < 0 || iters > 0) {
-      launch_spmv(p->qstencil(), obs, tau, x, p->d_r, nrhs, st);
-      resid_kernel<<<nblk, 256, 0, st>>>(b, p->d_r, ne, p->d_part);
-      p->launches_total += 2;
-      CUDA_TRY(cudaMemcpyAsync(part.data(), p->d_part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-      CUDA_TRY(cudaStreamSynchronize(st));
-      double r2 = 0.0, b2 = 0.0;
-      for (int k = 0; k < nblk; ++k) { r2 += part[2 * k]; b2 += part[2 * k + 1]; }
-      rel = b2 > 0 ? std::sqrt(r2 / b2) : std::sqrt(r2);
+    if (!fresh) {
+      rel = residual();
+      if (rel < 0) { p->last_error = "residual read-back failed"; return 2; }
     }
     *resid = rel;
   }
   CUDA_TRY(cudaGetLastError());
   if (p->profile) prof_collect(p);
-  if (tc_gemm_take_error(p->stream)) { p->last_error = "tensor-core product timed out"; return 2; }
+  if (tc_gemm_take_error(p->stream, p->pin_int() + 1)) { p->last_error = "tensor-core product timed out"; return 2; }
   return 0;
 }
 
@@ -1284,7 +1294,11 @@ static int selinv_t(Plan* p, double* zq) {
   p->launches_total += 1;
   CUDA_TRY(cudaStreamSynchronize(st));
   CUDA_TRY(cudaGetLastError());
-  if (tc_gemm_take_error(p->stream)) { p->last_error = "tensor-core product timed out"; p->factored = 0; return 2; }
+  if (tc_gemm_take_error(p->stream, p->pin_int() + 1)) {
+    p->last_error = "tensor-core product timed out";
+    p->factored = 0;
+    return 2;
+  }
   if (p->profile) prof_collect(p);
   p->factored = 0;  // the factor's panels now hold intermediate products
   return 0;

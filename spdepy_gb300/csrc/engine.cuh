@@ -151,6 +151,11 @@ struct Plan {
   int* d_err = nullptr;
   double* d_scalar = nullptr;  // small reduction outputs
   double* d_part = nullptr;    // block partial sums (1024)
+  // page-locked host buffer for the scalars and partial sums read back during a
+  // factorisation, solve or inversion: doubles 0-1023 partial sums, 1024 the
+  // log-pivot sum; ints at double 1536: the pivot error, the tensor-core flag
+  double* h_pin = nullptr;
+  int* pin_int() { return reinterpret_cast<int*>(h_pin + 1536); }
   // model / assembly state (FP64)
   DevModel model{};
   bool model_set = false;

@@ -64,13 +64,14 @@ void launch_gemm(const GemmTask* tasks, int ntasks, const T* A, const T* B, T* C
                  unsigned long long wait_ns = kTcWaitNs);
 
 // tcgen05 path for FP32 (tc_gemm.cu); tc_gemm_take_error returns and clears the
-// bounded-wait error flag of that kernel.
+// bounded-wait error flag of that kernel, read through `pinned` (page-locked host
+// memory, so that the copy does not serialise with other host threads' copies).
 void launch_gemm_tc(const GemmTask* tasks, int ntasks, const float* A, const float* B, float* C, int mode, int al,
                     int bl, cudaStream_t st, unsigned long long wait_ns = kTcWaitNs);
 // cluster-pair path (row-major A and B): one 2-CTA cluster per 256 x 256 task
 void launch_gemm_pair(const GemmTask* tasks, int ntasks, const CUtensorMap* maps, const float* A, const float* B,
                       float* C, int mode, cudaStream_t st, unsigned long long wait_ns = kTcWaitNs);
-int tc_gemm_take_error(cudaStream_t st);
+int tc_gemm_take_error(cudaStream_t st, int* pinned);
 bool tc_gemm_enabled();
 
 template <typename T>
@@ -78,6 +79,6 @@ void launch_potrf(const DiagTask* tasks, int ntasks, T* L, T* dinv, double* logp
 
 template <typename T>
 void launch_extend_add(const ExtendTask* tasks, int ntasks, const DevFront* fronts, const int* rmap, const T* U_child,
-                       T* L, T* U_parent, cudaStream_t st);
+                       T* L, T* U_parent, int max_r1, cudaStream_t st);
 
 }  // namespace spde

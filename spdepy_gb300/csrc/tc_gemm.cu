@@ -772,12 +772,13 @@ void launch_gemm_pair(const GemmTask* tasks, int ntasks, const CUtensorMap* maps
   }
 }
 
-int tc_gemm_take_error(cudaStream_t st) {
+int tc_gemm_take_error(cudaStream_t st, int* pinned) {
   // stream-ordered, so a second pipeline on another stream is not serialised
-  int h = 0;
   static const int z = 0;
-  cudaMemcpyFromSymbolAsync(&h, g_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
+  *pinned = 0;
+  cudaMemcpyFromSymbolAsync(pinned, g_tc_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
+  const int h = *pinned;
   if (h) {
     cudaMemcpyToSymbolAsync(g_tc_error, &z, sizeof(int), 0, cudaMemcpyHostToDevice, st);
     cudaStreamSynchronize(st);
