@@ -644,8 +644,26 @@ struct GWeights {
   const float* w;
   const uint32_t* mask;  // compact, with observations: observed nodes have their own rows
   const int* rank;
+  const uint32_t* near;  // with mask: bit p set when one of the 27 nodes p - d is observed
   int nob, Ns, T, compact;
 };
+
+// Bits of the nodes whose G^T row gathers from an observed node: p = q + d for
+// every observed q and offset d inside the grid.
+__global__ void near_obs_kernel(const int* __restrict__ nodes, int nob, int Mx, int Ny, int T,
+                                uint32_t* __restrict__ near) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nob) return;
+  const int Ns = Mx * Ny, q = nodes[j];
+  const int t = q / Ns, c = q - t * Ns, y = c / Mx, x = c - y * Mx;
+  for (int o = 0; o < kOff; ++o) {
+    const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+    const int xp = x + dx, yp = y + dy, tp = t + dt;
+    if (xp < 0 || xp >= Mx || yp < 0 || yp >= Ny || tp < 0 || tp >= T) continue;
+    const int p = (tp * Ny + yp) * Mx + xp;
+    atomicOr(&near[p >> 5], 1u << (p & 31));
+  }
+}
 
 // u = G r (TRANS 0) or z = G^T u with the block's partial sum of r . z
 // (TRANS 1) for column blockIdx.y, one thread per node; the rows of G come
@@ -682,14 +700,50 @@ __global__ void __launch_bounds__(256, 4) g32n_kernel(int Mx, int Ny, int T, GWe
       return w[(kc * kOff + o) * Ns + cq];
     };
     float acc = 0.f;
+    // interior node (all 27 neighbours exist and, for G^T, lie in the interior
+    // time class): no validity tests, rows found without per-offset lookups
+    const bool inner = xx >= 1 && xx + 1 < Mx && y >= 1 && y + 1 < Ny && t >= 1 + TRANS && t + 1 + TRANS < T &&
+                       (!TRANS || !COMPACT || !gw.mask || !((gw.near[p >> 5] >> (p & 31)) & 1u));
+    if (inner && !TRANS) {
+      const float* wr;
+      int stride;
+      if (!COMPACT) {
+        wr = w + p;
+        stride = n;
+      } else {
+        wr = w + kOff * Ns + c;
+        stride = Ns;
+        if (gw.mask) {
+          const uint32_t m = gw.mask[p >> 5], bit = 1u << (p & 31);
+          if (m & bit) {
+            wr = w + 3 * kOff * Ns + gw.rank[p >> 5] + __popc(m & (bit - 1u));
+            stride = gw.nob;
+          }
+        }
+      }
 #pragma unroll
-    for (int o = 0; o < kOff; ++o) {
-      const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
-      if (!((bx >> (dx + 1)) & (by >> (dy + 1)) & (bt >> (dt + 1)) & 1u)) continue;
-      const int d = dt * Ns + dy * Mx + dx;
-      const int q = TRANS ? p - d : p + d;
-      const float wv = TRANS ? wrow(q, t - dt, c - dy * Mx - dx, o) : wrow(p, t, c, o);
-      acc = fmaf(wv, x[q], acc);
+      for (int o = 0; o < kOff; ++o) {
+        const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+        acc = fmaf(wr[o * stride], x[p + dt * Ns + dy * Mx + dx], acc);
+      }
+    } else if (inner) {
+#pragma unroll
+      for (int o = 0; o < kOff; ++o) {
+        const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+        const int d = dt * Ns + dy * Mx + dx;
+        const float wv = COMPACT ? w[(kOff + o) * Ns + c - dy * Mx - dx] : w[o * n + p - d];
+        acc = fmaf(wv, x[p - d], acc);
+      }
+    } else {
+#pragma unroll
+      for (int o = 0; o < kOff; ++o) {
+        const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dt = o / 9 - 1;
+        if (!((bx >> (dx + 1)) & (by >> (dy + 1)) & (bt >> (dt + 1)) & 1u)) continue;
+        const int d = dt * Ns + dy * Mx + dx;
+        const int q = TRANS ? p - d : p + d;
+        const float wv = TRANS ? wrow(q, t - dt, c - dy * Mx - dx, o) : wrow(p, t, c, o);
+        acc = fmaf(wv, x[q], acc);
+      }
     }
     outv[int64_t(col) * n + p] = acc;
     if (TRANS) dot = rv[int64_t(col) * n + p] * acc;
@@ -1038,8 +1092,10 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
                         size_t(8 * nrhs) + size_t(nrhs);
   double* base = scratch(p, need64);
   // FP32 (column-major): r, z, p, Ap, x correction, G r; coefficients; observation term; alpha, beta
+  const bool near_bits = kind == 3 && with_obs;  // G^T needs the nodes next to observed ones
+  const size_t nwords = size_t((n + 31) / 32);
   const size_t need32 = size_t(6 * len) + size_t(kCoef32) * Ns + size_t(n) + size_t(2 * nrhs) +
-                        (kind == 4 ? size_t(kIcRow) * n : 0);
+                        (kind == 4 ? size_t(kIcRow) * n : 0) + (near_bits ? nwords : 0);
   float* b32 = scratch32(p, need32);
   if (!base || !b32) return 4;
   double* r64 = base;
@@ -1055,6 +1111,7 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
   float* alpha = o32 + n;
   float* beta = alpha + nrhs;
   float* Lic = beta + nrhs;  // IC(0) factor (kind 4)
+  uint32_t* near = reinterpret_cast<uint32_t*>(Lic + (kind == 4 ? size_t(kIcRow) * n : 0));
   const QStencil q = p->qstencil();
   const double* obs = with_obs ? p->d_obs_cnt : nullptr;
   const int sep = q.sep;
@@ -1073,7 +1130,12 @@ int pcg_solve(Plan* p, int with_obs, double tau, int kind, const float* w, const
     if (!ok) return 7;
     w += kCompactHeader;
   }
-  GWeights gw{w, (kind == 3 && with_obs) ? p->d_obs_mask : nullptr, p->d_obs_rank, p->nob, Ns, T, kind == 3 ? 1 : 0};
+  GWeights gw{w, near_bits ? p->d_obs_mask : nullptr, p->d_obs_rank, near_bits ? near : nullptr, p->nob, Ns, T,
+              kind == 3 ? 1 : 0};
+  if (near_bits) {
+    cudaMemsetAsync(near, 0, nwords * sizeof(uint32_t), st);
+    if (p->nob > 0) near_obs_kernel<<<nblk(p->nob), 256, 0, st>>>(p->d_obs_nodes, p->nob, Mx, Ny, T, near);
+  }
   coef32_kernel<<<nblk(Ns, 128), 128, 0, st>>>(q, cf);
   if (obs) obs32_kernel<<<nblk(n), 256, 0, st>>>(obs, tau, o32, n);
   const float* o = obs ? o32 : nullptr;
