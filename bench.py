@@ -36,8 +36,8 @@ METRIC = "logL+grad evals/s & samples/s, 200x200x24 SPDE: mixed+learned vs FP64 
 
 # DRAM bytes per algorithmic flop of the tensor-core product, from the ncu
 # capture of the largest cluster-pair launch at 100 x 100 x 24 (an inverse-block
-# product of 4.430e11 flops: 1.294e9 bytes read, 0.156e9 written).
-TC_DRAM_BYTES_PER_FLOP = 1.450e9 / 4.430e11
+# product of 4.430e11 flops: 1.285e9 bytes read, 0.157e9 written).
+TC_DRAM_BYTES_PER_FLOP = 1.442e9 / 4.430e11
 
 
 def _tf32_tflops(torch, n=8192, reps=10):
