@@ -34,6 +34,9 @@ namespace spde {
 constexpr int kNbk = 64;  // diagonal block size (kMaxNbk in dense.cu)
 constexpr int kTcMinK = 128;  // shortest K routed to the tensor-core product
 constexpr int kTcMinKUpdate = 64;  // ... for the rank-64 updates inside a factor panel
+// shortest K of a cluster-pair task: below it the pair's per-task set-up and
+// pipeline fill outweigh its throughput, and the single-CTA kernel is faster
+constexpr int kPairMinK = 256;
 enum { KT_NONE = 0, KT_A_UPPER, KT_B_LOWER, KT_BOTH_UPPER };
 constexpr int kPanel = 512;   // panel width of the two-level blocked factorisation
 
@@ -63,7 +66,7 @@ void Schedule::release() {
 struct Builder {
   Schedule& s;
   int TM, TN;
-  bool pair_ok;   // products of at least 128 x 128 x 128 may take 256 x 256 cluster-pair tiles (FP32 plan)
+  bool pair_ok;   // products of at least 128 x 128 x kPairMinK may take 256 x 256 cluster-pair tiles (FP32 plan)
   int depth = 0;  // tree depth of the ops begun next
   explicit Builder(Schedule& sc, int tm, int tn, bool pairs = false) : s(sc), TM(tm), TN(tn), pair_ok(pairs) {}
 
@@ -186,7 +189,7 @@ struct Builder {
   // K index shares the origin of their row index (KT_A_UPPER: A[i,k] = 0 for
   // k < i; KT_B_LOWER: B[j,k] = 0 for k > j; KT_BOTH_UPPER: both upper).
   // abase / bbase: start of the row-major region the operand lies in (for its
-  // TMA map); with both given, a product of at least 128 x 128 x 128 in the FP32
+  // TMA map); with both given, a product of at least 128 x 128 x kPairMinK in the FP32
   // plan takes 256 x 256 tiles for the cluster-pair tensor-core kernel.
   void gemm_tiles(int64_t a, int lda, int64_t arow, int64_t b, int ldb, int64_t brow, int64_t c, int ldc, int m, int n,
                   int k, bool lower = false, int i_start = 0, int kt = KT_NONE, int64_t abase = -1,
@@ -194,7 +197,7 @@ struct Builder {
     if (m <= 0 || n <= 0 || k <= 0) return;
     const Op& op = s.ops.back();
     const bool pair = pair_ok && abase >= 0 && bbase >= 0 && arow == lda && brow == ldb && op.al == kRow &&
-                      op.bl == kRow && m >= 128 && n >= 128 && k >= 128 && i_start == 0;
+                      op.bl == kRow && m >= 128 && n >= 128 && k >= kPairMinK && i_start == 0;
     const int tm = pair ? kPairTile : TM, tn = pair ? kPairTile : TN;
     for (int j0 = 0; j0 < n; j0 += tn)
       for (int i0 = lower ? std::max(j0, i_start) : i_start; i0 < m; i0 += tm) {
