@@ -134,10 +134,12 @@ int spde_plan_read_sites(SpdePlan* plan, double* ms, double* flops, int64_t* til
  * factor and inverse memory.  1 runs them one after the other on one set. */
 int spde_plan_set_pipelines(SpdePlan* plan, int pipelines);
 /* Failure detection (no reference counterpart): every wait inside the
- * tensor-core kernels gives up after this many nanoseconds of wall clock (0
- * restores the default, 2 s); the kernel then records an error, waits for its
- * issued tensor-core work, frees its tensor memory and returns, and the
- * factorisation or inversion returns SPDE_ERR_CUDA with the plan still usable.
+ * tensor-core kernels, and every wait of the one-right-hand-side triangular
+ * sweeps on another block's completion flag, gives up after this many
+ * nanoseconds of wall clock (0 restores the default, 2 s); the kernel then
+ * records an error (the tensor-core kernels wait for their issued tensor-core
+ * work and free their tensor memory first) and returns, and the factorisation,
+ * inversion, solve or sample returns SPDE_ERR_CUDA with the plan still usable.
  * Tests lower the limit to make the waits run out. */
 int spde_plan_set_wait_limit(SpdePlan* plan, int64_t ns);
 /* Symbolic analysis without a GPU (host only): statistics and the ordering. */

@@ -299,7 +299,7 @@ int spde_symbolic_export(int Mx, int Ny, int T, int leaf_max, int32_t* perm, int
 static void release_numeric(Plan& p) {
   void* ptrs[] = {p.d_fronts, p.d_perm, p.d_iperm, p.d_front_of, p.d_blist, p.d_rmap, p.d_amap, p.d_L, p.d_dinv,
                   p.d_pool[0], p.d_pool[1], p.d_logpiv, p.d_err, p.d_scalar, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0],
-                  p.d_G[1], p.d_r, p.d_x64, p.d_b64, p.d_part, p.d_sx, p.d_pc};
+                  p.d_G[1], p.d_r, p.d_x64, p.d_b64, p.d_part, p.d_sx, p.d_pc, p.d_chain, p.d_chain_err};
   for (void* q : ptrs) cudaFree(q);
   cudaFreeHost(p.h_pin);
   p.h_pin = nullptr;
@@ -431,7 +431,7 @@ int spde_plan_destroy(SpdePlan* plan) {
                   p.d_pool[0], p.d_pool[1], p.d_logpiv, p.d_err, p.d_scalar, p.d_bs, p.d_bsH, p.d_bsA, p.d_ww,
                   p.d_theta, p.d_Ageo, p.d_A0geo, p.d_kap, p.d_qs, p.d_Q0, p.d_QA, p.d_QO, p.d_cQs, p.d_obs_cnt,
                   p.d_obs_idx, p.d_X, p.d_W[0], p.d_W[1], p.d_G[0], p.d_G[1], p.d_r, p.d_x64, p.d_b64,
-                  p.d_obs_mask, p.d_obs_rank, p.d_obs_nodes, p.d_pc32};
+                  p.d_obs_mask, p.d_obs_rank, p.d_obs_nodes, p.d_pc32, p.d_chain, p.d_chain_err};
   for (void* q : ptrs) cudaFree(q);
   cudaFreeHost(p.h_pin);
   p.h_pin = nullptr;

@@ -362,9 +362,22 @@ static void build_factor_schedule(const Symbolic& S, Schedule& sc, int TM, int T
   }
 }
 
+// First completion flag of every front's 64-row blocks (one-column sweeps).
+static std::vector<int64_t> chain_bases(const Symbolic& S, int64_t* total) {
+  std::vector<int64_t> base(S.fronts.size());
+  int64_t t = 0;
+  for (size_t f = 0; f < S.fronts.size(); ++f) {
+    base[f] = t;
+    t += (S.fronts[f].ns + kNbk - 1) / kNbk;
+  }
+  if (total) *total = t;
+  return base;
+}
+
 static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, int nrhs) {
   Builder b(sc, TM, TN);
   const auto& F = S.fronts;
+  const std::vector<int64_t> chain_base = chain_bases(S, nullptr);
   const int chunk = std::max(1, std::min(nrhs, 16));
   for (int d = S.max_depth; d >= 0; --d) {
     const auto& fr = S.by_depth[d];
@@ -377,6 +390,26 @@ static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
     b.end();
     int steps = 0;
     for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
+    if (nrhs == 1) {
+      // one right-hand side: the level's block chain in one launch, then the
+      // border rows in one product: W[B] -= L_B y
+      Op& oc = b.begin(OP_FWD_CHAIN);
+      oc.depth = d;
+      for (int kb = 0; kb < steps; ++kb)
+        for (int f : fr)
+          if (F[f].ns > kb * kNbk) sc.rows.push_back({f, kb, int(chain_base[f])});
+      b.end();
+      Op& ob = b.begin(OP_GEMM);
+      ob.site = S_V_FWD_B; ob.mode = kSub; ob.al = kRow; ob.bl = kCol;
+      ob.abuf = B_L; ob.bbuf = B_X; ob.cbuf = pd == 0 ? B_W0 : B_W1;
+      for (int f : fr) {
+        const Front& x = F[f];
+        if (x.nb == 0 || x.ns == 0) continue;
+        b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld, x.ld, x.ld, int64_t(x.s0), 1, 1, x.w_base, 1, x.nb, 1, x.ns);
+      }
+      b.end();
+      continue;
+    }
     for (int kb = 0; kb < steps; ++kb) {
       Op& o1 = b.begin(OP_GEMM);  // y_k = Linv_k x_k (in place)
       o1.site = S_V_FWD_D; o1.mode = kStore; o1.al = kRow; o1.bl = kCol;
@@ -421,6 +454,7 @@ static void build_fwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
 static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, int nrhs) {
   Builder b(sc, TM, TN);
   const auto& F = S.fronts;
+  const std::vector<int64_t> chain_base = chain_bases(S, nullptr);
   const int chunk = std::max(1, std::min(nrhs, 16));
   for (int d = 0; d <= S.max_depth; ++d) {
     const auto& fr = S.by_depth[d];
@@ -444,6 +478,19 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
     b.end();
     int steps = 0;
     for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
+    if (nrhs == 1) {
+      // one right-hand side: the level's block chain in one launch, each front's
+      // blocks from its last one down
+      Op& oc = b.begin(OP_BWD_CHAIN);
+      oc.depth = d;
+      for (int r = 0; r < steps; ++r)
+        for (int f : fr) {
+          const int kb = nblocks(F[f].ns) - 1 - r;
+          if (kb >= 0) sc.rows.push_back({f, kb, int(chain_base[f])});
+        }
+      b.end();
+      continue;
+    }
     for (int kb = steps - 1; kb >= 0; --kb) {
       Op& o1 = b.begin(OP_GEMM);  // x_k = Linv_k^T x_k
       o1.site = S_V_BWD_D; o1.mode = kStore; o1.al = kCol; o1.bl = kCol;
@@ -685,6 +732,160 @@ static void build_selinv_schedule(const Symbolic& S, Schedule& sc, int TM, int T
     }
   }
   *scratch_elems = scratch;
+}
+
+// ------------------------------------------------------ one-column sweeps
+// The forward and backward substitutions of one tree level for a single right-
+// hand side, as one launch each instead of two launches per 64-column block:
+// block (front f, block k) of the level is a CTA that takes a ticket (so that
+// every block it waits for belongs to a CTA that has already started), folds in
+// the blocks it depends on as their completion flags appear, solves with the
+// 64 x 64 block inverse and publishes its flag.  Flags carry the sweep's epoch,
+// so they need no reset.  A wait gives up after wait_ns (the solve then reports
+// an error instead of hanging).
+__device__ __forceinline__ unsigned long long chain_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool chain_wait(const unsigned* flag, unsigned epoch, unsigned long long wait_ns) {
+  auto done = [&]() {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+    return int(v - epoch) >= 0;
+  };
+  if (done()) return true;
+  const unsigned long long t0 = chain_now();
+  while (!done()) {
+    if (chain_now() - t0 > wait_ns) return false;
+    __nanosleep(64);
+  }
+  return true;
+}
+__device__ __forceinline__ void chain_publish(unsigned* flag, unsigned epoch) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(flag), "r"(epoch) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ T load_cg(const T* p) {
+  return __ldcg(p);
+}
+
+// Forward: y_k = Linv_k (x_k - sum_{j<k} L_kj y_j) in place in X (tasks: front,
+// block k, flag base of the front; sorted by k).  Thread (row i, quarter q).
+template <typename T>
+__global__ void __launch_bounds__(256) fwd_chain_kernel(const RowTask* __restrict__ tasks,
+                                                        const DevFront* __restrict__ fronts, const T* __restrict__ L,
+                                                        const T* __restrict__ dinv, T* __restrict__ X,
+                                                        unsigned* __restrict__ flags, unsigned* __restrict__ counter,
+                                                        unsigned epoch, int* __restrict__ err,
+                                                        unsigned long long wait_ns) {
+  __shared__ T sD[64][65];
+  __shared__ T ys[64], acc[64];
+  __shared__ int ticket, fail;
+  const int tid = threadIdx.x, i = tid >> 2, q = tid & 3;
+  if (tid == 0) {
+    ticket = int(atomicAdd(counter, 1u));
+    fail = 0;
+  }
+  __syncthreads();
+  const RowTask tk = tasks[ticket];
+  const DevFront f = fronts[tk.front];
+  const int k = tk.r0, r0 = k * 64, w = min(64, f.ns - r0);
+  const T* Lrow = L + f.p_off + int64_t(r0 + (i < w ? i : 0)) * f.ld + q * 16;
+  for (int e = tid; e < 64 * 64; e += 256) {
+    const int a = e >> 6, b = e & 63;
+    sD[a][b] = (a < w && b < w) ? dinv[f.d_off + int64_t(k) * 64 * 64 + e] : T(0);
+  }
+  T part = 0;
+  for (int j = 0; j < k; ++j) {
+    if (tid == 0 && !chain_wait(flags + tk.r1 + j, epoch, wait_ns)) {
+      fail = 1;
+      atomicExch(err, 1);
+    }
+    __syncthreads();
+    if (tid < 64) ys[tid] = load_cg(X + f.s0 + j * 64 + tid);
+    __syncthreads();
+    if (fail) break;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) part += Lrow[j * 64 + c] * ys[q * 16 + c];
+  }
+  part += __shfl_xor_sync(0xffffffffu, part, 1);
+  part += __shfl_xor_sync(0xffffffffu, part, 2);
+  if (q == 0) acc[i] = i < w ? X[f.s0 + r0 + i] - part : T(0);
+  __syncthreads();
+  T y = 0;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) y += sD[i][q * 16 + c] * acc[q * 16 + c];
+  y += __shfl_xor_sync(0xffffffffu, y, 1);
+  y += __shfl_xor_sync(0xffffffffu, y, 2);
+  if (q == 0 && i < w) {
+    X[f.s0 + r0 + i] = y;
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) chain_publish(flags + tk.r1 + k, epoch);
+}
+
+// Backward: x_k = Linv_k^T (x_k - sum_{j>k} L_jk^T x_j) in place in X (tasks
+// sorted by the distance of k from the front's last block).  Thread (column c,
+// quarter q of the rows of block j).
+template <typename T>
+__global__ void __launch_bounds__(256) bwd_chain_kernel(const RowTask* __restrict__ tasks,
+                                                        const DevFront* __restrict__ fronts, const T* __restrict__ L,
+                                                        const T* __restrict__ dinv, T* __restrict__ X,
+                                                        unsigned* __restrict__ flags, unsigned* __restrict__ counter,
+                                                        unsigned epoch, int* __restrict__ err,
+                                                        unsigned long long wait_ns) {
+  __shared__ T sD[64][65];
+  __shared__ T xs[64], acc[64], red[4][64];
+  __shared__ int ticket, fail;
+  const int tid = threadIdx.x, c = tid & 63, q = tid >> 6;
+  if (tid == 0) {
+    ticket = int(atomicAdd(counter, 1u));
+    fail = 0;
+  }
+  __syncthreads();
+  const RowTask tk = tasks[ticket];
+  const DevFront f = fronts[tk.front];
+  const int k = tk.r0, c0 = k * 64, w = min(64, f.ns - c0);
+  const int nbk = (f.ns + 63) / 64;
+  for (int e = tid; e < 64 * 64; e += 256) {
+    const int a = e >> 6, b = e & 63;
+    sD[a][b] = (a < w && b < w) ? dinv[f.d_off + int64_t(k) * 64 * 64 + e] : T(0);
+  }
+  T part = 0;
+  for (int j = nbk - 1; j > k; --j) {
+    const int wj = min(64, f.ns - j * 64);
+    if (tid == 0 && !chain_wait(flags + tk.r1 + j, epoch, wait_ns)) {
+      fail = 1;
+      atomicExch(err, 1);
+    }
+    __syncthreads();
+    if (tid < 64) xs[tid] = tid < wj ? load_cg(X + f.s0 + j * 64 + tid) : T(0);
+    __syncthreads();
+    if (fail) break;
+    if (c < w) {
+      const T* Lb = L + f.p_off + int64_t(j * 64 + q * 16) * f.ld + c0 + c;
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        if (q * 16 + i < wj) part += Lb[int64_t(i) * f.ld] * xs[q * 16 + i];
+    }
+  }
+  red[q][c] = part;
+  __syncthreads();
+  if (tid < 64) acc[tid] = tid < w ? X[f.s0 + c0 + tid] - ((red[0][tid] + red[1][tid]) + (red[2][tid] + red[3][tid])) : T(0);
+  __syncthreads();
+  T x = 0;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) x += sD[q * 16 + i][c] * acc[q * 16 + i];
+  red[q][c] = x;
+  __syncthreads();
+  if (tid < w) {
+    X[f.s0 + c0 + tid] = (red[0][tid] + red[1][tid]) + (red[2][tid] + red[3][tid]);
+    __threadfence();
+  }
+  __syncthreads();
+  if (tid == 0) chain_publish(flags + tk.r1 + k, epoch);
 }
 
 // ------------------------------------------------------------ small kernels
@@ -987,12 +1188,28 @@ struct Exec {
         case OP_MIRROR:
           mirror_kernel<T><<<o.count, 256, 0, st>>>(s.d_mirror + o.off, buf(o.abuf), buf(o.cbuf));
           break;
+        case OP_FWD_CHAIN:
+        case OP_BWD_CHAIN: {
+          cudaMemsetAsync(p->d_chain, 0, sizeof(unsigned), st);
+          if (++p->chain_epoch == 0) ++p->chain_epoch;
+          if (o.kind == OP_FWD_CHAIN)
+            fwd_chain_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, buf(B_L), buf(B_DINV),
+                                                         buf(B_X), p->d_chain + 64, p->d_chain, p->chain_epoch,
+                                                         p->d_chain_err, p->tc_wait_ns);
+          else
+            bwd_chain_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, buf(B_L), buf(B_DINV),
+                                                         buf(B_X), p->d_chain + 64, p->d_chain, p->chain_epoch,
+                                                         p->d_chain_err, p->tc_wait_ns);
+          break;
+        }
         case OP_ZEXTRACT:
           zextract_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, p->d_iperm, p->d_amap,
                                                       p->sym.nslots, buf(o.cbuf), zq);
           break;
       }
-      if (timed) prof_end(p, st, on_tc ? kProfTensorCore : o.kind, o.flops, o.site, o.kind == OP_GEMM ? o.count : 0);
+      if (timed)
+        prof_end(p, st, on_tc ? kProfTensorCore : (o.kind >= OP_FWD_CHAIN ? int(OP_GEMM) : o.kind), o.flops, o.site,
+                 o.kind == OP_GEMM ? o.count : 0);
     }
     if (depth_log && !dmarks.empty()) {
       dmark(-1);
@@ -1118,6 +1335,13 @@ int plan_build(Plan* p) {
   CUDA_TRY(cudaMalloc(&p->d_scalar, 64 * sizeof(double)));
   CUDA_TRY(cudaMalloc(&p->d_part, 1024 * sizeof(double)));
   CUDA_TRY(cudaMallocHost(&p->h_pin, 2048 * sizeof(double)));
+  int64_t nflags = 0;
+  chain_bases(S, &nflags);
+  CUDA_TRY(cudaMalloc(&p->d_chain, size_t(64 + nflags) * sizeof(unsigned)));
+  CUDA_TRY(cudaMemset(p->d_chain, 0, size_t(64 + nflags) * sizeof(unsigned)));
+  CUDA_TRY(cudaMalloc(&p->d_chain_err, sizeof(int)));
+  CUDA_TRY(cudaMemset(p->d_chain_err, 0, sizeof(int)));
+  p->chain_epoch = 0;
   return 0;
 }
 
@@ -1201,6 +1425,20 @@ static void tri_solve(Plan* p, int nrhs) {
   Exec<T>{p, *bw, nrhs, nullptr}.run();
 }
 
+// Reads and clears the one-column sweeps' wait-failure flag (page-locked read-back).
+static int chain_take_error(Plan* p) {
+  int* h = p->pin_int() + 2;
+  *h = 0;
+  cudaMemcpyAsync(h, p->d_chain_err, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
+  cudaStreamSynchronize(p->stream);
+  const int e = *h;
+  if (e) {
+    cudaMemsetAsync(p->d_chain_err, 0, sizeof(int), p->stream);
+    cudaStreamSynchronize(p->stream);
+  }
+  return e;
+}
+
 template <typename T>
 static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, double tol, double* resid) {
   const int n = p->sym.n;
@@ -1252,6 +1490,7 @@ static int solve_t(Plan* p, const double* b, double* x, int nrhs, int iters, dou
   CUDA_TRY(cudaGetLastError());
   if (p->profile) prof_collect(p);
   if (tc_gemm_take_error(p->stream, p->pin_int() + 1)) { p->last_error = "tensor-core product timed out"; return 2; }
+  if (chain_take_error(p)) { p->last_error = "triangular sweep timed out"; return 2; }
   return 0;
 }
 
@@ -1272,6 +1511,7 @@ static int sample_t(Plan* p, const double* z, double* x, int nrhs) {
   p->launches_total += 2;
   CUDA_TRY(cudaGetLastError());
   if (p->profile) prof_collect(p);
+  if (nrhs == 1 && chain_take_error(p)) { p->last_error = "triangular sweep timed out"; return 2; }
   return 0;
 }
 

@@ -16,7 +16,8 @@
 namespace spde {
 
 enum OpKind {
-  OP_MEMSET = 0, OP_EXTEND, OP_DIAG, OP_GEMM, OP_SGATHER_FWD, OP_SGATHER_BWD, OP_ZGATHER, OP_MIRROR, OP_ZEXTRACT
+  OP_MEMSET = 0, OP_EXTEND, OP_DIAG, OP_GEMM, OP_SGATHER_FWD, OP_SGATHER_BWD, OP_ZGATHER, OP_MIRROR, OP_ZEXTRACT,
+  OP_FWD_CHAIN, OP_BWD_CHAIN
 };
 // profile class of a tiled product that ran on the tensor cores (the others count as OP_GEMM)
 constexpr int kProfTensorCore = 9;
@@ -149,6 +150,13 @@ struct Plan {
   int64_t pool_elems[2] = {0, 0};
   double* d_logpiv = nullptr;
   int* d_err = nullptr;
+  // one-column triangular sweeps (engine.cu, fwd_chain_kernel / bwd_chain_kernel):
+  // word 0 the block ticket counter, words 64.. one completion flag per 64-row
+  // block of every front (the epoch of the sweep that finished it); the error
+  // word is set when a wait on a flag gives up
+  unsigned* d_chain = nullptr;
+  unsigned chain_epoch = 0;
+  int* d_chain_err = nullptr;
   double* d_scalar = nullptr;  // small reduction outputs
   double* d_part = nullptr;    // block partial sums (1024)
   // page-locked host buffer for the scalars and partial sums read back during a

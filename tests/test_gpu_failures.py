@@ -131,3 +131,28 @@ def test_tensor_core_wait_limit_returns_an_error_and_the_plan_recovers():
         plan.solve(torch.zeros(w.grid.n, dtype=torch.float64))  # no valid factor
     ld1 = plan.factor(False, 0.0)
     assert ld1 == ld0
+
+
+def test_sweep_wait_limit_returns_an_error_and_the_plan_recovers():
+    """The one-right-hand-side sweeps wait on per-block completion flags with the
+    plan's wait limit.  With the limit lowered to 1 ns the waits give up, the
+    solve reports a timed-out sweep, and with the default limit restored the
+    same factor solves to the refinement tolerance."""
+    from spdepy_gb300 import _native as nat
+    from spdepy_gb300.workloads import build_model, nonstationary_advection_diffusion
+    w = nonstationary_advection_diffusion(M=48, N=48, T=12)
+    mod = build_model(w, "mixed")
+    mod._assemble(w.par)
+    plan = mod.plan
+    plan.factor(False, 0.0)
+    L = nat.lib()
+    b = torch.randn(w.grid.n, dtype=torch.float64, generator=torch.Generator().manual_seed(3))
+    nat.check(L.spde_plan_set_wait_limit(plan.h, 1), plan.h)
+    try:
+        with pytest.raises(nat.SpdeError, match="timed out"):
+            plan.solve(b, refine=0)
+    finally:
+        nat.check(L.spde_plan_set_wait_limit(plan.h, 0), plan.h)
+    x, res = plan.solve(b, refine=10, tol=1e-12)
+    assert res < 1e-10
+    assert torch.allclose(plan.spmv(x).cpu(), b, rtol=0, atol=1e-9 * b.abs().max())
