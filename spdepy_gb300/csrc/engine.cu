@@ -466,21 +466,12 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
       if (F[f].nb > 0)
         for (int r0 = 0; r0 < nrhs; r0 += chunk) sc.rows.push_back({f, r0, std::min(nrhs, r0 + chunk)});
     b.end();
-    Op& o0 = b.begin(OP_GEMM);  // x_S -= L_BS^T x_B
-    o0.site = S_V_BWD_0; o0.mode = kSub; o0.al = kCol; o0.bl = kCol;
-    o0.abuf = B_L; o0.bbuf = pd == 0 ? B_G0 : B_G1; o0.cbuf = B_X;
-    for (int f : fr) {
-      const Front& x = F[f];
-      if (x.nb == 0) continue;
-      b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld, x.ld, 1, x.w_base * nrhs, nrhs, 1, int64_t(x.s0) * nrhs, nrhs, x.ns,
-                   nrhs, x.nb);
-    }
-    b.end();
     int steps = 0;
     for (int f : fr) steps = std::max(steps, nblocks(F[f].ns));
     if (nrhs == 1) {
       // one right-hand side: the level's block chain in one launch, each front's
-      // blocks from its last one down
+      // blocks from its last one down; each block first takes its border term
+      // -L_BS^T x_B, which depends on no other block
       Op& oc = b.begin(OP_BWD_CHAIN);
       oc.depth = d;
       for (int r = 0; r < steps; ++r)
@@ -491,6 +482,16 @@ static void build_bwd_schedule(const Symbolic& S, Schedule& sc, int TM, int TN, 
       b.end();
       continue;
     }
+    Op& o0 = b.begin(OP_GEMM);  // x_S -= L_BS^T x_B
+    o0.site = S_V_BWD_0; o0.mode = kSub; o0.al = kCol; o0.bl = kCol;
+    o0.abuf = B_L; o0.bbuf = pd == 0 ? B_G0 : B_G1; o0.cbuf = B_X;
+    for (int f : fr) {
+      const Front& x = F[f];
+      if (x.nb == 0) continue;
+      b.gemm_tiles(x.p_off + int64_t(x.ns) * x.ld, x.ld, 1, x.w_base * nrhs, nrhs, 1, int64_t(x.s0) * nrhs, nrhs, x.ns,
+                   nrhs, x.nb);
+    }
+    b.end();
     for (int kb = steps - 1; kb >= 0; --kb) {
       Op& o1 = b.begin(OP_GEMM);  // x_k = Linv_k^T x_k
       o1.site = S_V_BWD_D; o1.mode = kStore; o1.al = kCol; o1.bl = kCol;
@@ -826,20 +827,21 @@ __global__ void __launch_bounds__(256) fwd_chain_kernel(const RowTask* __restric
   if (tid == 0) chain_publish(flags + tk.r1 + k, epoch);
 }
 
-// Backward: x_k = Linv_k^T (x_k - sum_{j>k} L_jk^T x_j) in place in X (tasks
-// sorted by the distance of k from the front's last block).  Thread (column c,
-// quarter q of the rows of block j).
+// Backward: x_k = Linv_k^T (x_k - L_Bk^T x_B - sum_{j>k} L_jk^T x_j) in place in
+// X (tasks sorted by the distance of k from the front's last block; x_B, the
+// border rows' solution from the parent, in G).  Thread (column c, row group g
+// of eight): the border term, which depends on no other block, comes first.
 template <typename T>
-__global__ void __launch_bounds__(256) bwd_chain_kernel(const RowTask* __restrict__ tasks,
+__global__ void __launch_bounds__(512) bwd_chain_kernel(const RowTask* __restrict__ tasks,
                                                         const DevFront* __restrict__ fronts, const T* __restrict__ L,
                                                         const T* __restrict__ dinv, T* __restrict__ X,
-                                                        unsigned* __restrict__ flags, unsigned* __restrict__ counter,
-                                                        unsigned epoch, int* __restrict__ err,
-                                                        unsigned long long wait_ns) {
+                                                        const T* __restrict__ G, unsigned* __restrict__ flags,
+                                                        unsigned* __restrict__ counter, unsigned epoch,
+                                                        int* __restrict__ err, unsigned long long wait_ns) {
   __shared__ T sD[64][65];
-  __shared__ T xs[64], acc[64], red[4][64];
+  __shared__ T xs[64], acc[64], red[8][64];
   __shared__ int ticket, fail;
-  const int tid = threadIdx.x, c = tid & 63, q = tid >> 6;
+  const int tid = threadIdx.x, c = tid & 63, g = tid >> 6;
   if (tid == 0) {
     ticket = int(atomicAdd(counter, 1u));
     fail = 0;
@@ -849,11 +851,24 @@ __global__ void __launch_bounds__(256) bwd_chain_kernel(const RowTask* __restric
   const DevFront f = fronts[tk.front];
   const int k = tk.r0, c0 = k * 64, w = min(64, f.ns - c0);
   const int nbk = (f.ns + 63) / 64;
-  for (int e = tid; e < 64 * 64; e += 256) {
+  for (int e = tid; e < 64 * 64; e += 512) {
     const int a = e >> 6, b = e & 63;
     sD[a][b] = (a < w && b < w) ? dinv[f.d_off + int64_t(k) * 64 * 64 + e] : T(0);
   }
+  // border rows b = g, g + 8, ...: eight rows in flight per thread
   T part = 0;
+  if (c < w && f.nb > 0) {
+    const T* Lb = L + f.p_off + int64_t(f.ns) * f.ld + c0 + c;
+    const T* xb = G + f.w_base;
+    T s8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int b = g;
+    for (; b + 56 < f.nb; b += 64) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) s8[u] += Lb[int64_t(b + 8 * u) * f.ld] * xb[b + 8 * u];
+    }
+    for (; b < f.nb; b += 8) s8[0] += Lb[int64_t(b) * f.ld] * xb[b];
+    part = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+  }
   for (int j = nbk - 1; j > k; --j) {
     const int wj = min(64, f.ns - j * 64);
     if (tid == 0 && !chain_wait(flags + tk.r1 + j, epoch, wait_ns)) {
@@ -865,23 +880,31 @@ __global__ void __launch_bounds__(256) bwd_chain_kernel(const RowTask* __restric
     __syncthreads();
     if (fail) break;
     if (c < w) {
-      const T* Lb = L + f.p_off + int64_t(j * 64 + q * 16) * f.ld + c0 + c;
+      const T* Lj = L + f.p_off + int64_t(j * 64 + g * 8) * f.ld + c0 + c;
 #pragma unroll
-      for (int i = 0; i < 16; ++i)
-        if (q * 16 + i < wj) part += Lb[int64_t(i) * f.ld] * xs[q * 16 + i];
+      for (int i = 0; i < 8; ++i)
+        if (g * 8 + i < wj) part += Lj[int64_t(i) * f.ld] * xs[g * 8 + i];
     }
   }
-  red[q][c] = part;
+  red[g][c] = part;
   __syncthreads();
-  if (tid < 64) acc[tid] = tid < w ? X[f.s0 + c0 + tid] - ((red[0][tid] + red[1][tid]) + (red[2][tid] + red[3][tid])) : T(0);
+  if (tid < 64) {
+    T t = 0;
+#pragma unroll
+    for (int h = 0; h < 8; ++h) t += red[h][tid];
+    acc[tid] = tid < w ? X[f.s0 + c0 + tid] - t : T(0);
+  }
   __syncthreads();
   T x = 0;
 #pragma unroll
-  for (int i = 0; i < 16; ++i) x += sD[q * 16 + i][c] * acc[q * 16 + i];
-  red[q][c] = x;
+  for (int i = 0; i < 8; ++i) x += sD[g * 8 + i][c] * acc[g * 8 + i];
+  red[g][c] = x;
   __syncthreads();
   if (tid < w) {
-    X[f.s0 + c0 + tid] = (red[0][tid] + red[1][tid]) + (red[2][tid] + red[3][tid]);
+    T t = 0;
+#pragma unroll
+    for (int h = 0; h < 8; ++h) t += red[h][tid];
+    X[f.s0 + c0 + tid] = t;
     __threadfence();
   }
   __syncthreads();
@@ -1197,8 +1220,9 @@ struct Exec {
                                                          buf(B_X), p->d_chain + 64, p->d_chain, p->chain_epoch,
                                                          p->d_chain_err, p->tc_wait_ns);
           else
-            bwd_chain_kernel<T><<<o.count, 256, 0, st>>>(s.d_rows + o.off, p->d_fronts, buf(B_L), buf(B_DINV),
-                                                         buf(B_X), p->d_chain + 64, p->d_chain, p->chain_epoch,
+            bwd_chain_kernel<T><<<o.count, 512, 0, st>>>(s.d_rows + o.off, p->d_fronts, buf(B_L), buf(B_DINV),
+                                                         buf(B_X), buf((o.depth & 1) == 0 ? B_G0 : B_G1),
+                                                         p->d_chain + 64, p->d_chain, p->chain_epoch,
                                                          p->d_chain_err, p->tc_wait_ns);
           break;
         }
