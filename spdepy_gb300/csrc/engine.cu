@@ -855,19 +855,62 @@ __global__ void __launch_bounds__(512) bwd_chain_kernel(const RowTask* __restric
     const int a = e >> 6, b = e & 63;
     sD[a][b] = (a < w && b < w) ? dinv[f.d_off + int64_t(k) * 64 * 64 + e] : T(0);
   }
-  // border rows b = g, g + 8, ...: eight rows in flight per thread
+  // border rows: FP32 rows with 16-byte aligned columns and the block's 64
+  // columns inside the row are read as float4 (thread: 4 columns, row group of
+  // 32, four rows in flight), the others one column per thread (row group of 8,
+  // eight rows in flight); either way a block sum per column lands in bsum
+  __shared__ T bsum[64];
   T part = 0;
-  if (c < w && f.nb > 0) {
-    const T* Lb = L + f.p_off + int64_t(f.ns) * f.ld + c0 + c;
-    const T* xb = G + f.w_base;
-    T s8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int b = g;
-    for (; b + 56 < f.nb; b += 64) {
+  const T* xb = G + f.w_base;
+  const bool vec = sizeof(T) == 4 && ((f.p_off | f.ld) & 3) == 0 && c0 + 64 <= f.ld;
+  if (f.nb > 0 && vec) {
+    __shared__ float red32[32][65];
+    const int cq = tid & 15, g2 = tid >> 4;
+    const float* Lb = reinterpret_cast<const float*>(L) + f.p_off + int64_t(f.ns) * f.ld + c0 + 4 * cq;
+    const float* xf = reinterpret_cast<const float*>(xb);
+    float4 s4[4];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) s8[u] += Lb[int64_t(b + 8 * u) * f.ld] * xb[b + 8 * u];
+    for (int u = 0; u < 4; ++u) s4[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+    int b = g2;
+    for (; b + 96 < f.nb; b += 128) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 l = *reinterpret_cast<const float4*>(Lb + int64_t(b + 32 * u) * f.ld);
+        const float xv = xf[b + 32 * u];
+        s4[u].x += l.x * xv; s4[u].y += l.y * xv; s4[u].z += l.z * xv; s4[u].w += l.w * xv;
+      }
     }
-    for (; b < f.nb; b += 8) s8[0] += Lb[int64_t(b) * f.ld] * xb[b];
-    part = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+    for (; b < f.nb; b += 32) {
+      const float4 l = *reinterpret_cast<const float4*>(Lb + int64_t(b) * f.ld);
+      const float xv = xf[b];
+      s4[0].x += l.x * xv; s4[0].y += l.y * xv; s4[0].z += l.z * xv; s4[0].w += l.w * xv;
+    }
+    red32[g2][4 * cq + 0] = (s4[0].x + s4[1].x) + (s4[2].x + s4[3].x);
+    red32[g2][4 * cq + 1] = (s4[0].y + s4[1].y) + (s4[2].y + s4[3].y);
+    red32[g2][4 * cq + 2] = (s4[0].z + s4[1].z) + (s4[2].z + s4[3].z);
+    red32[g2][4 * cq + 3] = (s4[0].w + s4[1].w) + (s4[2].w + s4[3].w);
+    __syncthreads();
+    if (tid < 64) {
+      float t = 0.f;
+#pragma unroll 8
+      for (int h = 0; h < 32; ++h) t += red32[h][tid];
+      bsum[tid] = T(t);
+    }
+  } else if (f.nb > 0) {
+    if (c < w) {
+      const T* Lb = L + f.p_off + int64_t(f.ns) * f.ld + c0 + c;
+      T s8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      int b = g;
+      for (; b + 56 < f.nb; b += 64) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s8[u] += Lb[int64_t(b + 8 * u) * f.ld] * xb[b + 8 * u];
+      }
+      for (; b < f.nb; b += 8) s8[0] += Lb[int64_t(b) * f.ld] * xb[b];
+      part = ((s8[0] + s8[1]) + (s8[2] + s8[3])) + ((s8[4] + s8[5]) + (s8[6] + s8[7]));
+    }
+    if (tid < 64) bsum[tid] = T(0);
+  } else if (tid < 64) {
+    bsum[tid] = T(0);
   }
   for (int j = nbk - 1; j > k; --j) {
     const int wj = min(64, f.ns - j * 64);
@@ -889,7 +932,7 @@ __global__ void __launch_bounds__(512) bwd_chain_kernel(const RowTask* __restric
   red[g][c] = part;
   __syncthreads();
   if (tid < 64) {
-    T t = 0;
+    T t = bsum[tid];
 #pragma unroll
     for (int h = 0; h < 8; ++h) t += red[h][tid];
     acc[tid] = tid < w ? X[f.s0 + c0 + tid] - t : T(0);
