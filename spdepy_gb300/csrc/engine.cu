@@ -1074,17 +1074,21 @@ __global__ void zsym_kernel(int Mx, int Ny, int T, int nslots, const int* __rest
   zq[e] = zq[nb * nslots + opp];
 }
 
+// Sum of the log pivots (FP64, fixed order: strided per thread, then a warp
+// shuffle tree, then the eight warp sums in order), one block of 256 threads.
 __global__ void sum_kernel(const double* __restrict__ v, int64_t n, double* __restrict__ out) {
-  __shared__ double red[256];
+  __shared__ double warp_sum[8];
   double s = 0.0;
   for (int64_t i = threadIdx.x; i < n; i += 256) s += v[i];
-  red[threadIdx.x] = s;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(0xffffffffu, s, d);
+  if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = s;
   __syncthreads();
-  for (int k = 128; k > 0; k >>= 1) {
-    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-    __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += warp_sum[w];
+    *out = t;
   }
-  if (threadIdx.x == 0) *out = red[0];
 }
 
 // r = b - r (in place on r), and partial sums of |r|^2 and |b|^2
@@ -1352,6 +1356,69 @@ static void encode_maps(Plan* p, Schedule& sc, const int64_t* sizes) {
   cudaMemcpy(sc.d_maps, host.data(), host.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
 }
 
+// ------------------------------------------------------ nested dissection
+// The fill-reducing ordering on the device: every lattice node descends the
+// geometric dissection tree of the (x, y, t) box by itself, with the splitting
+// rule of the symbolic analysis (symbolic.cpp, NDBuilder::build): the cheapest of
+// a thickness-2 cut across x or y and a thickness-1 cut across t, a box of at
+// most leaf_max nodes or with no admissible cut being a leaf.  A box's nodes are
+// numbered after both children's (post-order): child 1, child 2, then its own
+// separator, each box x-fastest.  The numbering of a node follows from the box
+// volumes alone, so no tree is stored.
+__global__ void nd_perm_kernel(int Mx, int Ny, int T, int leaf_max, int* __restrict__ perm,
+                               int* __restrict__ iperm) {
+  const int64_t n = int64_t(Mx) * Ny * T;
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int x = int(k % Mx), y = int((k / Mx) % Ny), t = int(k / (int64_t(Mx) * Ny));
+  int box[6] = {0, Mx, 0, Ny, 0, T};
+  int64_t base = 0;
+  const int64_t kInf = INT64_MAX;
+  for (int level = 0; level < 256; ++level) {
+    const int a = box[1] - box[0], b = box[3] - box[2], c = box[5] - box[4];
+    const int64_t vol = int64_t(a) * b * c;
+    const int64_t cx = a >= 4 ? int64_t(2) * b * c : kInf;
+    const int64_t cy = b >= 4 ? int64_t(2) * a * c : kInf;
+    const int64_t ct = (T > 1 && c >= 3) ? int64_t(a) * b : kInf;
+    const int64_t cmin = min(cx, min(cy, ct));
+    int sp[6] = {box[0], box[1], box[2], box[3], box[4], box[5]};
+    if (vol <= leaf_max || cmin == kInf) break;  // leaf: numbered below as a whole
+    int k1[6] = {box[0], box[1], box[2], box[3], box[4], box[5]};
+    int k2[6] = {box[0], box[1], box[2], box[3], box[4], box[5]};
+    if (cmin == cx) {
+      const int m = box[0] + (a - 2) / 2;
+      k1[1] = m; sp[0] = m; sp[1] = m + 2; k2[0] = m + 2;
+    } else if (cmin == cy) {
+      const int m = box[2] + (b - 2) / 2;
+      k1[3] = m; sp[2] = m; sp[3] = m + 2; k2[2] = m + 2;
+    } else {
+      const int m = box[4] + (c - 1) / 2;
+      k1[5] = m; sp[4] = m; sp[5] = m + 1; k2[4] = m + 1;
+    }
+    auto inside = [&](const int* q) {
+      return x >= q[0] && x < q[1] && y >= q[2] && y < q[3] && t >= q[4] && t < q[5];
+    };
+    const int64_t v1 = int64_t(k1[1] - k1[0]) * (k1[3] - k1[2]) * (k1[5] - k1[4]);
+    const int64_t v2 = int64_t(k2[1] - k2[0]) * (k2[3] - k2[2]) * (k2[5] - k2[4]);
+    if (inside(k1)) {
+      for (int e = 0; e < 6; ++e) box[e] = k1[e];
+      continue;
+    }
+    if (inside(k2)) {
+      base += v1;
+      for (int e = 0; e < 6; ++e) box[e] = k2[e];
+      continue;
+    }
+    base += v1 + v2;  // the separator, after both children
+    for (int e = 0; e < 6; ++e) box[e] = sp[e];
+    break;
+  }
+  const int wa = box[1] - box[0], wb = box[3] - box[2];
+  const int64_t v = base + (int64_t(t - box[4]) * wb + (y - box[2])) * wa + (x - box[0]);
+  perm[k] = int(v);
+  iperm[v] = int(k);
+}
+
 // ------------------------------------------------------------------- plan API
 int plan_build(Plan* p) {
   Symbolic& S = p->sym;
@@ -1371,8 +1438,20 @@ int plan_build(Plan* p) {
     d.child[0] = x.child[0]; d.child[1] = x.child[1];
   }
   p->d_fronts = upload_vec(df);
-  p->d_perm = upload_vec(S.perm);
-  p->d_iperm = upload_vec(S.iperm);
+  // the permutations come from the device ordering, checked against the
+  // symbolic analysis that laid out the fronts
+  CUDA_TRY(cudaMalloc(&p->d_perm, size_t(S.n) * sizeof(int)));
+  CUDA_TRY(cudaMalloc(&p->d_iperm, size_t(S.n) * sizeof(int)));
+  nd_perm_kernel<<<int((int64_t(S.n) + 255) / 256), 256>>>(S.Mx, S.Ny, S.T, S.leaf_max, p->d_perm, p->d_iperm);
+  CUDA_TRY(cudaGetLastError());
+  {
+    std::vector<int> dev(S.n);
+    CUDA_TRY(cudaMemcpy(dev.data(), p->d_perm, size_t(S.n) * sizeof(int), cudaMemcpyDeviceToHost));
+    if (dev != S.perm) {
+      p->last_error = "device nested-dissection ordering differs from the symbolic analysis";
+      return 2;
+    }
+  }
   p->d_front_of = upload_vec(S.front_of);
   p->d_blist = upload_vec(S.blist);
   p->d_rmap = upload_vec(S.rmap);

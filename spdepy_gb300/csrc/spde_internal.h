@@ -46,6 +46,7 @@ struct Symbolic {
   int n = 0;
   int nslots = kSlotsS;
   int nbk = 64;                 // diagonal block size of the blocked factorisation
+  int leaf_max = 0;             // largest box (nodes) kept as a leaf front
   std::vector<Front> fronts;    // post-order (children before parents)
   std::vector<int> perm;        // natural -> new
   std::vector<int> iperm;       // new -> natural

@@ -152,6 +152,7 @@ int build_symbolic(int Mx, int Ny, int T, int leaf_max, int nbk, Symbolic* out, 
   S.n = int(n64);
   S.nslots = separable ? kSlotsSep : (T > 1 ? kSlotsST : kSlotsS);
   S.nbk = nbk;
+  S.leaf_max = leaf_max;
   S.perm.assign(S.n, -1);
   NDBuilder B{&S, Mx, Ny, T, leaf_max};
   B.rt = separable ? 2 : 1;

@@ -222,3 +222,27 @@ def test_factor_handle_survives_other_factorisations():
     v = np.random.default_rng(3).normal(size=mod.grid.n)
     emp = np.mean((v @ xs) ** 2)
     assert emp == pytest.approx(v @ fac.solve_A(v), rel=0.15)
+
+
+@pytest.mark.parametrize("M,N,T,leaf", [(7, 5, 3, 16), (33, 17, 9, 64), (41, 29, 6, 128)])
+def test_device_ordering_on_odd_lattices(M, N, T, leaf):
+    """The plan's permutation comes from the device nested-dissection kernel and
+    is checked against the symbolic analysis when the plan is built; on lattices
+    with odd extents and small leaves the factor then solves Q x = b to the
+    refinement tolerance through that permutation, in both precisions."""
+    from spdepy_gb300.spdes import GPUPlan
+    from spdepy_gb300.workloads import build_model, nonstationary_advection_diffusion
+    w = nonstationary_advection_diffusion(M=M, N=N, T=T)
+    for precision in ("fp64", "mixed"):
+        mod = build_model(w, precision)
+        mod._plan = GPUPlan(w.grid, precision, leaf)
+        mod._model_key = None
+        mod._assemble(w.par)
+        plan = mod.plan
+        assert plan.info().n == M * N * T
+        plan.factor(False, 0.0)
+        b = torch.randn(w.grid.n, 2, dtype=torch.float64, generator=torch.Generator().manual_seed(M))
+        for rhs in (b[:, :1].contiguous(), b):
+            x, res = plan.solve(rhs, refine=10, tol=1e-12)
+            assert res < 1e-10, (precision, rhs.shape, res)
+            assert torch.allclose(plan.spmv(x).cpu(), rhs, rtol=0, atol=1e-9 * rhs.abs().max())
