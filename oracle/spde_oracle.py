@@ -16,7 +16,7 @@ Reference files followed (paths inside the reference project):
   model.py:73-87,120-127                                          sample / update
 
 Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
-import this module.  It is the checker, never the product path.
+import this module.  It is test infrastructure, never the product path.
 """
 from __future__ import annotations
 

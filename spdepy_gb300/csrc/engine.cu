@@ -1302,7 +1302,7 @@ struct Exec {
 };
 
 // ------------------------------------------------------------- TMA maps
-// cuTensorMapEncodeTiled, from the driver through the runtime (no libcuda link)
+// cuTensorMapEncodeTiled, the CUDA driver API entry point obtained through the runtime (no libcuda link)
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void* f = nullptr;

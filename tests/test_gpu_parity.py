@@ -13,7 +13,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 # tolerances: FP64 path is pinned to rounding; the mixed path (FP32 factor with
-# FP64 pivots and FP64 iterative refinement) to the benchmark spec's bound 1e-6 relative
+# FP64 pivots and FP64 iterative refinement) to 1e-6 relative, the mixed plan's accuracy bound
 TOL_F = {"fp64": 1e-11, "mixed": 1e-6}
 TOL_G = {"fp64": 1e-8, "mixed": 1e-4}
 
