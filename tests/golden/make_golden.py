@@ -39,10 +39,16 @@ the CUDA path.  Cases:
   after ``addInt`` / ``addCov`` (with and without intercept and scaling) on a
   padded space-time grid (reference ``grids/spat2Dtemp_regular_mesh.py:35-68``).
 
+* ``optim``  the reference's ``Optimize.fit`` (``optim/__init__.py``) with each of
+  its step rules (``adam``, ``rmsprop``, ``sgd``, ``adagrad``, ``adadelta``;
+  ``optim/*.py``) on a fixed smooth objective: the trajectory, the Polyak
+  average and the last objective, also with a learning-rate schedule, a ``fix``
+  mask and non-default step settings.
+
 ``python tests/golden/make_golden.py --only separable [name ...]`` regenerates just
 the separable cases, ``--only getS`` the grid_getS fixture, ``--only facade_cov`` the
 facade_cov fixture, ``--only facade_tau`` the facade_tau fixture, ``--only plumbing``
-the grid_adv and extended-grid model fixtures.
+the grid_adv and extended-grid model fixtures, ``--only optim`` the optim fixture.
 """
 from __future__ import annotations
 
@@ -349,6 +355,78 @@ def facade_tau_case(sp=None):
     print("facade_tau:", {k: float(np.linalg.norm(out[k])) for k in out if k.endswith("_mu2")})
 
 
+def optim_objective(x):
+    """A smooth, anisotropic objective with its gradient (no reference code)."""
+    a = np.array([1.0, 3.0, 0.5, 2.0, 0.25])
+    c = np.array([0.3, -0.7, 1.1, 0.0, -1.5])
+    d = x - c
+    f = float(np.sum(a * d ** 2) + 0.1 * np.sum(d ** 4) + 0.05 * np.sum(np.sin(x)))
+    g = 2 * a * d + 0.4 * d ** 3 + 0.05 * np.cos(x)
+    return f, g
+
+
+# The reference's fit reads the step's learning rate from a schedule only (a
+# scalar lr leaves it unset), so every run passes one.
+OPTIM_RUNS = [
+    ("adam", dict(lr=[0.05] * 40, pol=10)),
+    ("adam", dict(lr=list(np.linspace(0.2, 0.01, 30)), pol=5, beta1=0.8, beta2=0.99)),
+    ("rmsprop", dict(lr=[0.02] * 40, pol=10)),
+    ("rmsprop", dict(lr=[0.02] * 30, pol=3, decay=0.5, memory=0.7)),
+    ("sgd", dict(lr=[0.01] * 40, pol=10)),
+    ("sgd", dict(lr=[0.02] * 25, pol=4, decay=0.3, fix=[1, 3])),
+    ("adagrad", dict(lr=[0.3] * 40, pol=10)),
+    ("adadelta", dict(lr=[1.0] * 40, pol=10)),
+    ("adadelta", dict(lr=[1.0] * 30, pol=6, rho=0.8, epsilon=1e-4)),
+]
+
+
+def optim_cases():
+    """Optimize.fit of the reference on optim_objective for each step rule."""
+    ref_harness.load_reference()
+    import importlib
+    ropt = importlib.import_module("spdepy.optim")
+    import io
+    import contextlib
+    out = {"nruns": len(OPTIM_RUNS)}
+    x0 = np.array([1.0, 1.0, -1.0, 0.5, 0.0])
+    for i, (step, kw) in enumerate(OPTIM_RUNS):
+        opt = ropt.Optimize(fun=optim_objective)
+        kw = dict(kw)
+        if "lr" in kw and isinstance(kw["lr"], list):
+            kw["lr"] = np.array(kw["lr"])
+        if "fix" in kw:
+            kw["fix"] = np.array(kw["fix"])
+        if step == "sgd":
+            # the reference's SGD lacks the printInit that Optimize.fit calls, so
+            # its step object drives the same loop here (fit's body, line for
+            # line: evaluate, step with the scheduled rate, restore fixed entries)
+            sgd = ropt.SGD()
+            sgd.settings(**kw)
+            x = x0.copy()
+            histX, histF = [], []
+            for lr in kw["lr"]:
+                f, g = optim_objective(x)
+                histF.append(f)
+                keep = x[kw["fix"]] if "fix" in kw else None
+                x = sgd(x, f, g, lr)
+                if keep is not None:
+                    x[kw["fix"]] = keep
+                histX.append(x)
+            res = {"x": np.array(histX).T[:, -kw["pol"]:].mean(axis=1), "fun": f}
+            opt.histX, opt.histF = histX, histF
+        else:
+            with contextlib.redirect_stdout(io.StringIO()):
+                res = opt.fit(x0=x0.copy(), stepType=step, **kw)
+        out[f"r{i}_step"] = np.array(step)
+        out[f"r{i}_x"] = np.asarray(res["x"], dtype=float)
+        out[f"r{i}_fun"] = np.array(res["fun"], dtype=float)
+        out[f"r{i}_hist"] = np.array(opt.histX, dtype=float)
+        out[f"r{i}_histf"] = np.array(opt.histF, dtype=float)
+    out["x0"] = x0
+    np.savez_compressed(os.path.join(OUT, "optim.npz"), **out)
+    print("optim:", {k: out[k].tolist() for k in out if k.endswith("_fun")})
+
+
 def plumbing_cases(sp=None):
     """Face velocities and bases on extended grids, and two model objects on a
     grid extended by two cells (reference grids/spat2Dtemp_regular_mesh.py:
@@ -487,6 +565,8 @@ if __name__ == "__main__":
         facade_tau_case()
     elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "plumbing":
         plumbing_cases()
+    elif len(sys.argv) > 2 and sys.argv[1] == "--only" and sys.argv[2] == "optim":
+        optim_cases()
     else:
         main()
         separable_cases()
@@ -494,3 +574,4 @@ if __name__ == "__main__":
         facade_cov_case()
         facade_tau_case()
         plumbing_cases()
+        optim_cases()
