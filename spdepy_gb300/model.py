@@ -62,6 +62,8 @@ class Model:
         x0 = self.mod.initFit(data, **kwargs)
         if kwargs.get("x0") is None:
             kwargs["x0"] = x0
+        if kwargs.get("verbose") is not None and hasattr(self.mod, "print"):
+            kwargs["print"] = self.mod.print
         res = self.optim.fit(**kwargs)
         self.setQ(par=res["x"])
         return res

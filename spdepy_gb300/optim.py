@@ -145,8 +145,12 @@ class Optimize:
         self.step = make_step(step_type, kw)
         self.histX, self.histF, self.histJac = [], [], []
         f = jac = None
+        verbose = bool(kw.get("verbose"))
+        show = kw.get("print")
         for it in range(steps):
             f, jac = fun(x)
+            if verbose:  # the reference's progress line (optim/__init__.py, fitviz)
+                print("# %3.0d" % it, "| fun = %2.4f" % f, show(x) if show is not None else "")
             self.histF.append(f)
             self.histJac.append(jac)
             step_lr = lr[it] if hasattr(lr, "__len__") else lr

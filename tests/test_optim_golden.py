@@ -56,3 +56,12 @@ def test_unknown_step_rule_is_refused():
     from spdepy_gb300.optim import Optimize
     with pytest.raises(ValueError, match="not recognized"):
         Optimize(fun=_objective).fit(x0=np.zeros(5), stepType="newton", lr=[0.1])
+
+
+def test_verbose_prints_the_reference_progress_line(capsys):
+    from spdepy_gb300.optim import Optimize
+    g = load("optim.npz")
+    Optimize(fun=_objective).fit(x0=g["x0"].copy(), stepType="adam", lr=[0.05] * 3, pol=2, verbose=True,
+                                 print=lambda x: "x0 = %.2f" % x[0])
+    out = capsys.readouterr().out.splitlines()
+    assert len(out) == 3 and out[0].startswith("#   ") and "| fun = " in out[0] and "x0 = 1.00" in out[0]
