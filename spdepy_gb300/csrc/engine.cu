@@ -1022,20 +1022,34 @@ __global__ void zgather_kernel(const RowTask* __restrict__ tasks, const DevFront
   for (; bcol < f.nb; bcol += 32) dst[bcol] = src[rm[bcol]];
 }
 
+// 32 x 32 block copies, kMirrorTiles tasks per CTA: all their loads first, then
+// all their stores, so that a CTA keeps several tiles in flight (the tasks of one
+// launch never read what another writes)
+constexpr int kMirrorTiles = 4;
 template <typename T>
-__global__ void mirror_kernel(const MirrorTask* __restrict__ tasks, const T* src, T* dst) {
-  __shared__ T tile[32][33];
-  const MirrorTask tk = tasks[blockIdx.x];
+__global__ void mirror_kernel(const MirrorTask* __restrict__ tasks, int ntasks, const T* src, T* dst) {
+  __shared__ T tile[kMirrorTiles][32][33];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-  for (int i = ty; i < 32; i += 8)
-    if (i < tk.rows && tx < tk.cols) tile[i][tx] = src[tk.src + int64_t(i) * tk.lds + tx];
-  __syncthreads();
-  if (tk.trans) {
-    for (int j = ty; j < 32; j += 8)
-      if (j < tk.cols && tx < tk.rows) dst[tk.dst + int64_t(j) * tk.ldd + tx] = tile[tx][j];
-  } else {
+  const int t0 = blockIdx.x * kMirrorTiles;
+#pragma unroll
+  for (int u = 0; u < kMirrorTiles; ++u) {
+    if (t0 + u >= ntasks) break;
+    const MirrorTask tk = tasks[t0 + u];
     for (int i = ty; i < 32; i += 8)
-      if (i < tk.rows && tx < tk.cols) dst[tk.dst + int64_t(i) * tk.ldd + tx] = tile[i][tx];
+      if (i < tk.rows && tx < tk.cols) tile[u][i][tx] = src[tk.src + int64_t(i) * tk.lds + tx];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < kMirrorTiles; ++u) {
+    if (t0 + u >= ntasks) break;
+    const MirrorTask tk = tasks[t0 + u];
+    if (tk.trans) {
+      for (int j = ty; j < 32; j += 8)
+        if (j < tk.cols && tx < tk.rows) dst[tk.dst + int64_t(j) * tk.ldd + tx] = tile[u][tx][j];
+    } else {
+      for (int i = ty; i < 32; i += 8)
+        if (i < tk.rows && tx < tk.cols) dst[tk.dst + int64_t(i) * tk.ldd + tx] = tile[u][i][tx];
+    }
   }
 }
 
@@ -1256,7 +1270,8 @@ struct Exec {
           break;
         }
         case OP_MIRROR:
-          mirror_kernel<T><<<o.count, 256, 0, st>>>(s.d_mirror + o.off, buf(o.abuf), buf(o.cbuf));
+          mirror_kernel<T><<<(o.count + kMirrorTiles - 1) / kMirrorTiles, 256, 0, st>>>(s.d_mirror + o.off, o.count,
+                                                                                         buf(o.abuf), buf(o.cbuf));
           break;
         case OP_FWD_CHAIN:
         case OP_BWD_CHAIN: {
