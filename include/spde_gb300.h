@@ -129,9 +129,13 @@ int spde_plan_read_profile(SpdePlan* plan, double* ms, double* flops, int64_t* c
 int spde_plan_read_sites(SpdePlan* plan, double* ms, double* flops, int64_t* tiles, int reset);
 /* Concurrency of spde_loglike (no reference counterpart): with 2 pipelines (the
  * default) Q + tau S^T S is factored, solved and inverted on a second set of
- * arenas with its own stream and host thread while Q runs on the plan's own, so
- * the two factorisations' latency-bound top levels overlap; it doubles the
- * factor and inverse memory.  1 runs them one after the other on one set. */
+ * arenas with its own host thread while Q runs on the plan's own, so the two
+ * factorisations' latency-bound top levels overlap; it doubles the factor and
+ * inverse memory.  Each pipeline then runs its factorisation and solve on a
+ * greatest-priority stream and its inversion on a least-priority stream of the
+ * plan, ordered after the work already on the plan's stream and joined back to
+ * it before spde_loglike returns.  1 runs them one after the other on the plan's
+ * stream and one set of arenas. */
 int spde_plan_set_pipelines(SpdePlan* plan, int pipelines);
 /* Failure detection (no reference counterpart): every wait inside the
  * tensor-core kernels, and every wait of the one-right-hand-side triangular
